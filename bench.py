@@ -1,0 +1,274 @@
+"""Benchmark of the SPH-erosion simulation step on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload plain_1m]
+
+A step is one simulation step (sort, density, forces, integration, terrain
+contact, erosion) of every particle of the workload.  The default workload
+is the plain scene at scale: 1,048,576 particles over a 1024 x 1024 fBm
+terrain (see sph-erosion_gb300/workloads.py).  `value` is particle-steps/s
+with the state resident in HBM, each timed step bracketed by CUDA events on
+the library's stream and preceded by an L2 flush; `e2e` is the same metric
+through the C ABI with a parameter upload and a positions readback to host
+memory inside every timed step.  `--impl reference` times the reference's
+algorithm (the oracle's FP32 restatement of FluidSystemSPH::Run, all-pairs)
+on the host cores over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sph-erosion_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "particle-steps/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("LOCAL_RANK", "0"),
+                                          f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value, ws):
+    """Barrier and max over ranks (replicas only: no data-path collective)."""
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(spec, budget_s=12.0, nthreads=0):
+    """The reference's algorithm (all-pairs FP32, the oracle's restatement of
+    FluidSystemSPH::Run) on a bounded sample: the three passes and the
+    integration for m particles against all n.  Returns particle-steps/s."""
+    import oracle as O
+
+    p = spec["params"]
+    bh = p["box_half"]
+    prm = O.make_params(g=p["gravity"], dt=p["dt"], p0=p["rest_density"], mass=p["mass"], visc=p["viscosity"],
+                        surf_tens=p["surface_tension"], k=p["gas_stiffness"], cr=p["restitution"],
+                        h=p["smoothing_radius"], box_l=bh)
+    pos = spec["pos"]
+    vel = np.zeros_like(pos)
+    n = len(pos)
+    cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+    m = min(n, 64)
+    t0 = time.perf_counter()
+    O.time_sample(prm, pos, vel, n // 2, m, nthreads)
+    t = time.perf_counter() - t0
+    m2 = int(min(n, max(m, m * budget_s / max(t, 1e-6))))
+    i0 = max(0, n // 2 - m2 // 2)
+    t0 = time.perf_counter()
+    O.time_sample(prm, pos, vel, i0, m2, nthreads)
+    t = time.perf_counter() - t0
+    return m2 / t, cores, m2, t
+
+
+def run_reference(args, spec, config):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+
+    O.build()
+    vals = []
+    cores = m = 0
+    for _ in range(args.warmup):
+        pass
+    for _ in range(args.steps):
+        v, cores, m, _t = cpu_sample(spec, budget_s=args.ref_seconds)
+        vals.append(v)
+    val = float(np.median(vals))
+    line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": spec["n"] / val * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded lattice + fBm terrain)", "config": config,
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{m} of {spec['n']} particles x 3 all-pairs passes + integration per step"},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def flush_l2(buf):
+    buf.zero_()
+
+
+def run_ours(args, spec, config):
+    import torch
+
+    import sph_gb300 as S
+    import workloads as W
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    n = spec["n"]
+    sysm = S.System(particle_capacity=n, key_capacity=1 << 20, terrain_capacity=1 << 21, tile=args.tile,
+                    graph_steps=16, device=local)
+    sc = W.build_scene(sysm, spec)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    # warm-up
+    for _ in range(args.warmup):
+        sysm.step(1)
+    sysm.sync()
+    torch.cuda.synchronize()
+    # timed: K steps, each bracketed by CUDA events on the library stream,
+    # an L2 flush before each
+    with Clocks() as clk:
+        tot = 0.0
+        for _ in range(args.steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            tot += sysm.time_steps(1)
+        tot_s = barrier_max(tot / 1e3, ws)
+    value = ws * n * args.steps / tot_s
+    # per-stage device times of the same steps (events on the launching stream)
+    stages = sysm.profile_stages(max(3, min(args.steps, 10)))
+    # e2e: through the C ABI with host buffers, copies inside the timed region
+    prm = sc.params()
+    host_pos = np.zeros((n, 3), np.float32)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sc.set_params(prm)  # H2D: the parameter block, as the front end re-uploads edits each frame
+        sysm.step(1)
+        sc.get_positions(host_pos)  # D2H: positions for drawing
+    e2e_t = barrier_max(time.perf_counter() - t0, ws)
+    e2e = ws * n * args.steps / e2e_t
+    d = sc.diag()
+    if rank != 0:
+        return
+    # roofline of the dominant kernel (the force stage): algorithmic bytes =
+    # 48 B read (sorted pos, vel, density factors) + 32 B written (pos, vel)
+    # per particle + 4 B per terrain height read
+    hbm, kind = peaks()
+    t = spec.get("terrain")
+    texels = t["w"] * t["d"] if t else 0
+    force_ms = float(stages[5])
+    force_bytes = 80.0 * n + 4.0 * texels
+    achieved = force_bytes / (force_ms * 1e-3) / 1e9
+    step_ms = tot / args.steps
+    ncells = int(np.prod(sc.grid_dims()[:3]))
+    step_bytes = 88.0 * n + 16.0 * ncells + 20.0 * texels
+    cpu_v, cores, m, _ = cpu_sample(spec, budget_s=args.ref_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + fBm terrain)",
+        "config": config,
+        "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": kind,
+                     "step_bytes_frac": step_bytes / (step_ms * 1e-3) / 1e9 / hbm},
+        "cpu_baseline": {"value": cpu_v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{m} of {n} particles x 3 all-pairs passes + integration per step"},
+        "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": int(C_PARAMS_BYTES),
+                "d2h_bytes_per_step": int(n * 12)},
+        "gpu_launches": int(args.steps * (7 if t else 6)),
+        "stages_ms": {name: float(v) for name, v in zip(S.STAGES, stages)},
+        "clocks": clk.summary(),
+        "mass_units_total": int(d["total_units"]),
+    }
+    print(json.dumps(line), flush=True)
+
+
+C_PARAMS_BYTES = 4 * 24
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain_1m", choices=["plain_1m", "plain_small"])
+    ap.add_argument("--tile", type=int, default=256)
+    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    args = ap.parse_args()
+    import workloads as W
+
+    spec = W.plain_1m() if args.workload == "plain_1m" else W.plain_small()
+    t = spec.get("terrain")
+    config = {"workload": spec["name"], "particles": spec["n"],
+              "terrain": f"{t['w']}x{t['d']} fBm {t['octaves']} oct amp {t['amplitude']}" if t else None,
+              "box": "x".join(str(2 * b) for b in spec["params"]["box_half"]), "h": spec["params"]["smoothing_radius"],
+              "dt": spec["params"]["dt"], "erosion": bool(spec["params"]["erosion"]), "resort": "every step",
+              "l2": "flushed (512 MiB write) before every timed step"}
+    if args.impl == "reference":
+        run_reference(args, spec, config)
+    else:
+        run_ours(args, spec, config)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+/* sph_erosion.h - C ABI of the GB300 SPH-erosion simulation step.
+ *
+ * Every entry point returns an int status (SPH_OK = 0, negative on error);
+ * sph_last_error() gives the message of the calling thread's last failure.
+ * No C++ exception crosses this boundary and no device code traps.  Calls
+ * on one system handle are not thread-safe; different handles are.
+ *
+ * A system owns one CUDA stream and the device memory of all of its scenes.
+ * A scene is one independent fluid + terrain simulation (the state of one
+ * reference FluidSystemSPH plus its Grid).  sph_system_step advances every
+ * active scene of a system in one launch per stage.
+ *
+ * Each declaration names the reference interface it replaces
+ * (Erosion/fluid_system.h and Erosion/grid.h of victor-kataev/SPH-Erosion).
+ */
+#ifndef SPH_EROSION_H
+#define SPH_EROSION_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SPH_API __attribute__((visibility("default")))
+#else
+#define SPH_API
+#endif
+
+#define SPH_OK 0
+#define SPH_ERR_INVALID (-1)   /* bad argument or handle */
+#define SPH_ERR_CUDA (-2)      /* a CUDA call failed */
+#define SPH_ERR_NOMEM (-3)     /* device or host allocation failed */
+#define SPH_ERR_CAPACITY (-4)  /* request exceeds a configured capacity or budget */
+#define SPH_ERR_STATE (-5)     /* call not valid in the current state */
+#define SPH_ERR_DEVICE (-6)    /* a kernel reported an error status */
+
+/* flags of sph_params.flags */
+#define SPH_FLAG_RECORD 1  /* keep every FluidParticle field of the last step (GetParticle) */
+#define SPH_FLAG_ORDERED 2 /* sum each particle's neighbours in ascending id order (validation) */
+
+typedef struct sph_system sph_system;
+
+/* Simulation parameters: the members of FluidSystemSPH
+ * (Erosion/fluid_system.h:460-479) plus the box, grid and erosion settings
+ * that the reference hard-codes or lacks. */
+typedef struct sph_params {
+    float gravity[3];       /* g */
+    float dt;               /* deltaT; 0 = paused (fluid_system.h:342) */
+    float rest_density;     /* p0 */
+    float mass;             /* MASS */
+    float viscosity;        /* visc */
+    float surface_tension;  /* surf_tens */
+    float gas_stiffness;    /* k */
+    float restitution;      /* cR, used by the terrain contact */
+    float smoothing_radius; /* h */
+    float box_center[3];    /* the reference box is centred at 0 ... */
+    float box_half[3];      /* ... with half extent len on every axis */
+    float cell_mult;        /* uniform-grid cell edge / h, >= 0.5 (default 1) */
+    int erosion;            /* 1 = exchange sediment with the terrain */
+    float k_capacity;       /* carried volume fraction per m/s of speed */
+    float k_pickup;         /* 1/s */
+    float k_deposit;        /* 1/s */
+    float erosion_layer;    /* contact layer above the surface, metres */
+    int flags;              /* SPH_FLAG_* */
+} sph_params;
+
+/* One particle record, field for field the reference's FluidParticle
+ * (Erosion/fluid_system.h:49-64), plus the carried sediment. */
+typedef struct sph_particle {
+    int id;
+    float position[3];
+    float velocity[3];
+    float acceleration[3];
+    float density;
+    float pressure;
+    float pressure_force[3];
+    float viscosity_force[3];
+    float gravity_force[3];
+    float surface_force[3];
+    float surface_normal[3];
+    int neighb_id;
+    int32_t sediment; /* fixed-point units, see sph_scene_diag */
+} sph_particle;
+
+/* FP64 diagnostics of one scene (the only FP64 on the device). */
+typedef struct sph_diag {
+    double fluid_mass;     /* n * mass */
+    double momentum[3];    /* sum m v */
+    double kinetic;        /* sum m |v|^2 / 2 */
+    double potential;      /* sum -m (g . x) */
+    int64_t sediment_units;  /* sum of carried sediment */
+    int64_t terrain_units;   /* sum of terrain deltas */
+    int64_t total_units;     /* sediment + terrain: conserved exactly */
+    double unit_volume;      /* m^3 per unit */
+    int32_t n;               /* particles */
+    int32_t nan_particles;   /* particles with a non-finite position */
+} sph_diag;
+
+typedef struct sph_system_config {
+    int device;               /* CUDA ordinal */
+    int64_t particle_capacity; /* initial arena sizes; grown on demand */
+    int64_t key_capacity;
+    int64_t terrain_capacity;
+    int max_scenes;
+    int tile;                 /* particles per work tile: 128, 256 or 512 (0 = 256) */
+    int graph_steps;          /* steps per captured CUDA graph (0 = no graphs) */
+    int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
+} sph_system_config;
+
+/* ---- errors and defaults ------------------------------------------------ */
+SPH_API const char* sph_last_error(void);
+/* Fills the reference's member defaults (fluid_system.h:460-479): g = (0,-9.82,0),
+ * deltaT = 0, p0 = 998.29, MASS = 0.02, visc = 3.5, surf_tens = 0.0728, k = 3,
+ * cR = 0.5, h = 0.0457, box = [-0.2, 0.2]^3; erosion off. */
+SPH_API void sph_params_default(sph_params* p);
+SPH_API void sph_system_config_default(sph_system_config* c);
+
+/* ---- system --------------------------------------------------------------- */
+SPH_API int sph_system_create(const sph_system_config* cfg, sph_system** out);
+SPH_API int sph_system_destroy(sph_system* s);
+/* Advance every active scene nsteps (FluidSystemSPH::Run, fluid_system.h:104-183,
+ * once per step).  Enqueued on the system's stream; returns without waiting. */
+SPH_API int sph_system_step(sph_system* s, int nsteps);
+SPH_API int sph_system_sync(sph_system* s);
+/* Device time of nsteps steps measured with CUDA events on the system stream. */
+SPH_API int sph_system_time_steps(sph_system* s, int nsteps, float* ms);
+/* Device time per stage of one step, averaged over nsteps (stages: keys, scan,
+ * scatter, reorder, density, force, terrain, tick); ms must hold 8 floats. */
+SPH_API int sph_system_profile_stages(sph_system* s, int nsteps, float* ms);
+/* Bytes of device memory the system holds. */
+SPH_API int sph_system_memory(sph_system* s, int64_t* bytes);
+
+/* ---- scenes (one FluidSystemSPH + Grid each) ------------------------------ */
+/* FluidSystemSPH() (fluid_system.h:69-72): a scene with no particles.
+ * terrain_w/terrain_d = 0 for no terrain; capacity is a hint. */
+SPH_API int sph_scene_create(sph_system* s, const sph_params* p, int capacity, int terrain_w, int terrain_d,
+                     int* scene);
+SPH_API int sph_scene_destroy(sph_system* s, int scene);
+/* Writes through GetMass/GetVisc/GetSurfTen/Getp0/GetGrav (fluid_system.h:261-284)
+ * and SetDeltaTime (:216-219) become one parameter upload. */
+SPH_API int sph_scene_set_params(sph_system* s, int scene, const sph_params* p);
+SPH_API int sph_scene_get_params(sph_system* s, int scene, sph_params* p);
+/* Steps the scene still takes in sph_system_step; -1 = unlimited (default). */
+SPH_API int sph_scene_set_steps(sph_system* s, int scene, int steps);
+SPH_API int sph_scene_get_steps(sph_system* s, int scene, int* steps);
+/* Replace all particles: ids 0..n-1, zero sediment.  vel may be NULL. */
+SPH_API int sph_scene_set_particles(sph_system* s, int scene, int n, const float* pos3, const float* vel3);
+/* Initialize(n) / AddParticles(n) (fluid_system.h:74-102, :232-251): append a
+ * ceil(cbrt(n))^3 lattice at spacing 0.025 from (-0.2,-0.05,-0.15)+origin. */
+SPH_API int sph_scene_add_lattice(sph_system* s, int scene, int n, const float origin[3], int* added);
+SPH_API int sph_scene_count(sph_system* s, int scene, int* n);
+/* Positions, velocities, densities and sediment in id order (any may be NULL). */
+SPH_API int sph_scene_get_particles(sph_system* s, int scene, float* pos3, float* vel3, float* density,
+                            int32_t* sediment);
+/* GetParticle(id) (fluid_system.h:286-289).  Force fields are filled when the
+ * scene has SPH_FLAG_RECORD, zero otherwise. */
+SPH_API int sph_scene_get_particle(sph_system* s, int scene, int id, sph_particle* out);
+/* All records in id order (SPH_FLAG_RECORD): 27 floats each, laid out as
+ * pos3 vel3 acc3 density pressure fpress3 fvisc3 fgrav3 fsurf3 normal3 pad. */
+SPH_API int sph_scene_get_records(sph_system* s, int scene, float* rec27, int* neighb_id);
+SPH_API int sph_scene_diag(sph_system* s, int scene, sph_diag* out);
+
+/* ---- terrain (Grid heightfield, grid.h:43-116) ---------------------------- */
+/* LoadHeightfield generalised to any size and FP32 metres above the box floor
+ * (grid.h:98-102); resets the int64 erosion deltas to zero. */
+SPH_API int sph_scene_set_terrain(sph_system* s, int scene, int w, int d, const float* heights);
+/* Seeded fBm value noise (kind 0) or ridged fBm (kind 1) of the given
+ * octaves, amplitude, lacunarity and gain (the repository's own generator). */
+SPH_API int sph_scene_gen_terrain(sph_system* s, int scene, uint64_t seed, int octaves, float amplitude,
+                          float lacunarity, float gain, int kind);
+/* Current heights (base + delta) and the int64 deltas (either may be NULL). */
+SPH_API int sph_scene_get_terrain(sph_system* s, int scene, float* heights, int64_t* delta);
+SPH_API int sph_scene_terrain_dims(sph_system* s, int scene, int* w, int* d);
+
+/* ---- inspection for parity checks ---------------------------------------- */
+/* Cell key of each particle and the stable sorted order (ids), as the next
+ * step's sort computes them from the current positions. */
+SPH_API int sph_scene_debug_sort(sph_system* s, int scene, uint32_t* keys_by_id, int32_t* sorted_ids);
+/* In-range neighbour count (|x_i - x_j| <= h, j != i; fluid_system.h:139-142)
+ * of each particle, in id order, from the uniform-grid traversal. */
+SPH_API int sph_scene_neighbour_counts(sph_system* s, int scene, int32_t* counts_by_id);
+/* Grid dims used by the sort: nx ny nz nkeys. */
+SPH_API int sph_scene_grid_dims(sph_system* s, int scene, int* dims4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

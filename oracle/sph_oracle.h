@@ -1,0 +1,110 @@
+/* Test infrastructure only: the oracle for the SPH-erosion simulation step.
+ *
+ * A CPU restatement, in plain C, of the reference's FluidSystemSPH::Run
+ * (Erosion/fluid_system.h:104-183) with its kernels (:410-453), integration
+ * and box collision (:306-407), in two precisions:
+ *   - FP32 in the reference's exact operation order (all-pairs, ascending j),
+ *     which must agree bit for bit with the reference built headless;
+ *   - FP64 with the same constants, used to state each field's rounding error.
+ * It also restates the repository's own extensions, which have no reference
+ * code: the heightfield terrain contact, the erosion exchange in int64 fixed
+ * point, the cell keys and stable counting sort, and the seeded fBm terrain.
+ *
+ * Only tests, the smoke check and the CPU-baseline leg of the benchmark load
+ * this library, always as the checker; the product never does.
+ */
+#ifndef SPH_ORACLE_H
+#define SPH_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Scene parameters.  The reference case is box_c = 0, box_l = (len,len,len),
+ * terrain and erosion off. */
+typedef struct oracle_params {
+    float g[3];
+    float dt;
+    float p0;          /* rest density */
+    float mass;
+    float visc;
+    float surf_tens;
+    float k;           /* gas stiffness */
+    float cr;          /* restitution used by the terrain contact */
+    float h;           /* smoothing radius */
+    float box_c[3];    /* box centre */
+    float box_l[3];    /* box half extents */
+    /* terrain: vertex grid tw (along x) by td (along z) over the box floor */
+    int terrain;       /* 0 = off */
+    int tw, td;
+    float height_unit; /* metres of height per sediment unit on one vertex */
+    /* erosion */
+    int erosion;       /* 0 = off */
+    float k_capacity;  /* carried-volume fraction per (m/s) of speed */
+    float k_pickup;    /* 1/s */
+    float k_deposit;   /* 1/s */
+    float layer;       /* contact layer thickness above the surface (m) */
+} oracle_params;
+
+/* One per-particle record, the fields of FluidParticle (fluid_system.h:49-64):
+ * pos[3] vel[3] acc[3] density pressure fpress[3] fvisc[3] fgrav[3] fsurf[3]
+ * normal[3] pad  -> 27 floats. */
+#define ORACLE_REC 27
+
+/* Advance nsteps.  pos/vel: 3n floats (in/out).  nbid: n ints (in/out,
+ * NeighbId semantics).  sed: n int32 sediment units (in/out, may be null when
+ * erosion is off).  base: tw*td float heights above the box floor; delta:
+ * tw*td int64 units (in/out).  rec: n*ORACLE_REC floats of the last step
+ * (may be null).  nthreads <= 0 means all. */
+void oracle_run_f32(const oracle_params* p, int n, float* pos, float* vel, int* nbid, int32_t* sed,
+                    const float* base, int64_t* delta, float* rec, int nsteps, int nthreads);
+/* As oracle_run_f32 with correctly rounded x^2 and x^3 in place of powf. */
+void oracle_run_f32x(const oracle_params* p, int n, float* pos, float* vel, int* nbid, int32_t* sed,
+                     const float* base, int64_t* delta, float* rec, int nsteps, int nthreads);
+void oracle_run_f64(const oracle_params* p, int n, double* pos, double* vel, int* nbid, int32_t* sed,
+                    const float* base, int64_t* delta, double* rec, int nsteps, int nthreads);
+
+/* Timing sample for the CPU baseline: the reference's three all-pairs passes
+ * and the integration for particles [i0, i0+m) against all n particles
+ * (densities of the other particles are taken as p0).  Writes nothing back. */
+double oracle_time_sample(const oracle_params* p, int n, const float* pos, const float* vel, int i0, int m,
+                          int nthreads);
+
+/* Neighbour counts with the reference's test |x_i - x_j| <= h, j != i. */
+void oracle_neighbour_counts(int n, const float* pos, float h, int* counts, int nthreads);
+
+/* Uniform-grid restatement: cell dims, Morton-row keys and stable order. */
+typedef struct oracle_grid {
+    int nx, ny, nz;
+    int by, bz;        /* bits of the y and z Morton interleave */
+    int nkeys;         /* nx << (by+bz), plus one sentinel key */
+    float cell;        /* cell edge */
+    float inv_cell;
+    float lo[3];       /* grid origin (box minimum) */
+} oracle_grid;
+void oracle_grid_make(const oracle_params* p, float cell_mult, oracle_grid* g);
+uint32_t oracle_cell_key(const oracle_grid* g, float x, float y, float z);
+void oracle_cell_keys(const oracle_grid* g, int n, const float* pos, uint32_t* keys);
+/* perm[r] = index of the r-th particle in (key, index) order. */
+void oracle_stable_sort(int n, const uint32_t* keys, int nkeys, int* perm);
+
+/* Seeded fBm value-noise heightmap (the repository's own generator):
+ * kind 0 = value fBm, 1 = ridged fBm.  out: w*d floats, metres. */
+void oracle_fbm(uint64_t seed, int w, int d, int octaves, float amplitude, float lacunarity, float gain,
+                int kind, float* out);
+
+/* Reference lattice: Initialize(n) / AddParticles(n) positions
+ * (fluid_system.h:74-102, :232-251).  Returns the count written. */
+int oracle_lattice(int n, const float* origin, float* pos_out, int cap);
+
+/* Surface mesh of Grid::UpdateGrid (grid.h:138-176) for an 8-bit map of
+ * side 512 (x-major): verts 6 floats per (x,z), indices per genIndices. */
+int oracle_mesh(const unsigned char* map, int dimx, int dimy, int dimz, float* verts, unsigned* idx,
+                int idx_cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

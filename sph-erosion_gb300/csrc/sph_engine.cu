@@ -1,0 +1,1060 @@
+// Host engine: arenas, scenes, work lists, step orchestration, CUDA graphs.
+#include "sph_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace sph {
+
+void check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    const int code = (e == cudaErrorMemoryAllocation) ? SPH_ERR_NOMEM : SPH_ERR_CUDA;
+    throw Error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+constexpr int kPAlign = kMaxTile;  // particle ranges start on a tile boundary for every tile size
+constexpr int64_t kTAlign = kMaxTile;
+
+int64_t round_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+
+int bits_for(int n) {
+    int b = 0;
+    while ((1 << b) < n) ++b;
+    return b;
+}
+
+uint32_t yz_interleave(int cy, int cz, int by, int bz) {
+    uint32_t m = 0;
+    int o = 0;
+    const int top = std::max(by, bz);
+    for (int b = 0; b < top; ++b) {
+        if (b < by) m |= (uint32_t)((cy >> b) & 1) << o++;
+        if (b < bz) m |= (uint32_t)((cz >> b) & 1) << o++;
+    }
+    return m;
+}
+
+inline float bits_to_float(int v) {
+    float f;
+    std::memcpy(&f, &v, sizeof f);
+    return f;
+}
+inline int float_to_bits(float f) {
+    int v;
+    std::memcpy(&v, &f, sizeof v);
+    return v;
+}
+
+}  // namespace
+
+// Largest float s with sqrtf(s) <= h.  sqrtf is correctly rounded and
+// monotonic, so for every float s >= 0: sqrtf(s) <= h  <=>  s <= smax.  The
+// kernels test the squared distance against it, which selects exactly the
+// reference's neighbours (glm::length(r) <= h, fluid_system.h:119) without a
+// square root per candidate.
+float smax_for(float h) {
+    float s = h * h;
+    while (std::sqrt(s) > h) s = std::nextafter(s, 0.0f);
+    for (;;) {
+        float nx = std::nextafter(s, INFINITY);
+        if (std::sqrt(nx) <= h)
+            s = nx;
+        else
+            break;
+    }
+    return s;
+}
+
+// Smallest float f whose double value is >= 1e-4: for any float d,
+// (double)d < 10e-5 (fluid_system.h:438)  <=>  d < threshold.
+float coincidence_threshold() {
+    float f = (float)1e-4;
+    while ((double)f < 1e-4) f = std::nextafter(f, INFINITY);
+    for (;;) {
+        float pv = std::nextafter(f, 0.0f);
+        if ((double)pv >= 1e-4)
+            f = pv;
+        else
+            break;
+    }
+    return f;
+}
+
+// ---- RangeAlloc -------------------------------------------------------------
+void RangeAlloc::reset(int64_t cap) {
+    free_.clear();
+    cap_ = cap;
+    used_ = 0;
+    if (cap > 0) free_[0] = cap;
+}
+
+bool RangeAlloc::alloc(int64_t len, int64_t* off) {
+    if (len <= 0) {
+        *off = 0;
+        return true;
+    }
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= len) {
+            *off = it->first;
+            const int64_t rest = it->second - len, roff = it->first + len;
+            free_.erase(it);
+            if (rest > 0) free_[roff] = rest;
+            used_ += len;
+            return true;
+        }
+    }
+    return false;
+}
+
+void RangeAlloc::release(int64_t off, int64_t len) {
+    if (len <= 0) return;
+    used_ -= len;
+    auto it = free_.emplace(off, len).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            free_.erase(it);
+        }
+    }
+}
+
+void RangeAlloc::grow(int64_t cap) {
+    if (cap <= cap_) return;
+    const int64_t old = cap_;
+    cap_ = cap;
+    used_ += cap - old;  // release() below subtracts the new space again
+    release(old, cap - old);
+}
+
+// ---- DevBuf -------------------------------------------------------------------
+template <class T>
+void DevBuf<T>::resize(int64_t cnt, bool keep, cudaStream_t st) {
+    if (cnt == n) return;
+    T* np = nullptr;
+    if (cnt > 0) {
+        SPH_CK(cudaMalloc(&np, (size_t)cnt * sizeof(T)));
+        SPH_CK(cudaMemsetAsync(np, 0, (size_t)cnt * sizeof(T), st));
+        if (keep && p && n > 0)
+            SPH_CK(cudaMemcpyAsync(np, p, (size_t)std::min(n, cnt) * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        SPH_CK(cudaStreamSynchronize(st));
+    }
+    if (p) cudaFree(p);
+    p = np;
+    n = cnt;
+}
+
+template <class T>
+void DevBuf<T>::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+}
+
+// ---- System -----------------------------------------------------------------
+System::System(const sph_system_config& cfg) : cfg_(cfg) {
+    if (cfg_.tile == 0) cfg_.tile = 256;
+    if (cfg_.tile != 128 && cfg_.tile != 256 && cfg_.tile != 512)
+        throw Error(SPH_ERR_INVALID, "tile must be 128, 256 or 512");
+    if (cfg_.max_scenes <= 0) cfg_.max_scenes = 1024;
+    dev_ = cfg_.device;
+    SPH_CK(cudaSetDevice(dev_));
+    SPH_CK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
+    SPH_CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    pa_.reset(0);
+    ka_.reset(0);
+    ca_.reset(0);
+    ta_.reset(0);
+    tba_.reset(0);
+    dscenes_.resize(cfg_.max_scenes, false, st_);
+    steps_.resize(cfg_.max_scenes, false, st_);
+    nwork_.resize(4, false, st_);
+    slist_.resize(cfg_.max_scenes, false, st_);
+    status_.resize(1, false, st_);
+    diag_part_.resize((int64_t)kDiagBlocks * kDiagDoubles, false, st_);
+    diag_i_.resize(2, false, st_);
+    diag_nan_.resize(1, false, st_);
+    grow_particles(std::max<int64_t>(round_up(std::max<int64_t>(cfg_.particle_capacity, 1), kPAlign), kPAlign));
+    grow_keys(std::max<int64_t>(round_up(std::max<int64_t>(cfg_.key_capacity, 1), kChunk), kChunk));
+    grow_chunks(1024);
+    grow_tables(4096);
+    grow_terrain(std::max<int64_t>(round_up(std::max<int64_t>(cfg_.terrain_capacity, 1), kTAlign), kTAlign));
+}
+
+System::~System() {
+    drop_graph();
+    if (st_) cudaStreamSynchronize(st_);
+    DevBuf<float4>* f4[] = {&pos_, &vel_, &spos_, &svel_, &dyn_};
+    for (auto* b : f4) b->release();
+    key_.release(); slot_.release(); perm_.release();
+    nbid_.release(); snbid_.release(); rec_.release();
+    counts_.release(); offsets_.release(); chunk_.release(); tab_.release();
+    tbase_.release(); theight_.release(); tdelta_.release();
+    dscenes_.release(); steps_.release(); ptiles_.release(); ctiles_.release(); ttiles_.release();
+    nwork_.release(); slist_.release(); status_.release(); scratch_i_.release();
+    diag_part_.release(); diag_i_.release(); diag_nan_.release();
+    if (st_) cudaStreamDestroy(st_);
+}
+
+Scene& System::scene(int id) {
+    if (id < 0 || id >= (int)scenes_.size() || !scenes_[id].live) throw Error(SPH_ERR_INVALID, "no such scene");
+    return scenes_[id];
+}
+const Scene& System::scene(int id) const {
+    if (id < 0 || id >= (int)scenes_.size() || !scenes_[id].live) throw Error(SPH_ERR_INVALID, "no such scene");
+    return scenes_[id];
+}
+
+int64_t System::memory_bytes() const {
+    int64_t b = 0;
+    b += pos_.bytes() + vel_.bytes() + spos_.bytes() + svel_.bytes() + dyn_.bytes();
+    b += key_.bytes() + slot_.bytes() + perm_.bytes() + nbid_.bytes() + snbid_.bytes() + rec_.bytes();
+    b += counts_.bytes() + offsets_.bytes() + chunk_.bytes() + tab_.bytes();
+    b += tbase_.bytes() + theight_.bytes() + tdelta_.bytes();
+    b += dscenes_.bytes() + steps_.bytes() + ptiles_.bytes() + ctiles_.bytes() + ttiles_.bytes();
+    b += scratch_i_.bytes();
+    return b;
+}
+
+// Bytes one scene of n particles and a tw x td terrain needs in the arenas.
+int64_t System::scene_bytes(int n, int tw, int td, const sph_params& p) const {
+    Scene tmp;
+    tmp.prm = p;
+    const_cast<System*>(this)->geometry(tmp);
+    const int64_t pcap = round_up(std::max(n, 1), kPAlign);
+    const int64_t per_p = 5 * 16 + 3 * 4 + 2 * 4 + ((p.flags & SPH_FLAG_RECORD) ? kRecFloats * 4 : 0);
+    return pcap * per_p + (int64_t)tmp.k_cap * 8 + (int64_t)tmp.nchunks * 4 + tmp.tab_len * 4 +
+           round_up((int64_t)tw * td, kTAlign) * 16 + (int64_t)(pcap / cfg_.tile + tmp.nchunks) * 8;
+}
+
+void System::check_budget(int64_t extra) const {
+    if (cfg_.hbm_budget > 0 && memory_bytes() + extra > cfg_.hbm_budget)
+        throw Error(SPH_ERR_CAPACITY, "HBM budget exceeded");
+}
+
+void System::drop_graph() {
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    gexec_ = nullptr;
+    graph_ = nullptr;
+    graph_dirty_ = true;
+}
+
+void System::grow_particles(int64_t cap) {
+    const int64_t need = cap - pos_.n;
+    if (need <= 0) return;
+    check_budget(need * (5 * 16 + 3 * 4 + 2 * 4 + (rec_.n ? kRecFloats * 4 : 0)));
+    DevBuf<float4>* f4[] = {&pos_, &vel_, &spos_, &svel_, &dyn_};
+    for (auto* b : f4) b->resize(cap, true, st_);
+    key_.resize(cap, true, st_);
+    slot_.resize(cap, true, st_);
+    perm_.resize(cap, true, st_);
+    nbid_.resize(cap, true, st_);
+    snbid_.resize(cap, true, st_);
+    if (rec_.n) rec_.resize(cap * kRecFloats, true, st_);
+    pa_.grow(cap);
+    drop_graph();
+}
+void System::grow_keys(int64_t cap) {
+    if (cap <= counts_.n) return;
+    check_budget((cap - counts_.n) * 8);
+    counts_.resize(cap, true, st_);
+    offsets_.resize(cap, true, st_);
+    ka_.grow(cap);
+    drop_graph();
+}
+void System::grow_chunks(int64_t cap) {
+    if (cap <= chunk_.n) return;
+    chunk_.resize(cap, true, st_);
+    ca_.grow(cap);
+    drop_graph();
+}
+void System::grow_tables(int64_t cap) {
+    if (cap <= tab_.n) return;
+    tab_.resize(cap, true, st_);
+    tba_.grow(cap);
+    drop_graph();
+}
+void System::grow_terrain(int64_t cap) {
+    if (cap <= tbase_.n) return;
+    check_budget((cap - tbase_.n) * 16);
+    tbase_.resize(cap, true, st_);
+    theight_.resize(cap, true, st_);
+    tdelta_.resize(cap, true, st_);
+    ta_.grow(cap);
+    drop_graph();
+}
+
+// which: 0 particles, 1 keys, 2 chunks, 3 tables, 4 terrain
+void System::ensure_arena(RangeAlloc& ra, int64_t need, int which) {
+    int64_t off;
+    if (ra.alloc(need, &off)) {
+        ra.release(off, need);
+        return;
+    }
+    const int64_t cap = std::max(ra.cap() * 2, ra.cap() + need);
+    switch (which) {
+        case 0: grow_particles(round_up(cap, kPAlign)); break;
+        case 1: grow_keys(round_up(cap, kChunk)); break;
+        case 2: grow_chunks(cap); break;
+        case 3: grow_tables(cap); break;
+        default: grow_terrain(round_up(cap, kTAlign)); break;
+    }
+}
+
+// Uniform grid of a scene.  Cell edge = h * cell_mult * (1 + 2^-12); the
+// slack keeps any two particles within h at most `reach` cells apart after
+// the FP32 rounding of the key arithmetic, so the traversal never misses a
+// neighbour.
+void System::geometry(Scene& sc) {
+    const sph_params& p = sc.prm;
+    sc.cell = (p.smoothing_radius * p.cell_mult) * 1.000244140625f;
+    sc.inv_cell = 1.0f / sc.cell;
+    int d[3];
+    for (int a = 0; a < 3; ++a) {
+        const float ext = p.box_half[a] + p.box_half[a];
+        int nd = (int)std::ceil((double)ext / (double)sc.cell);
+        d[a] = std::max(nd, 1);
+        sc.lo[a] = p.box_center[a] - p.box_half[a];
+    }
+    sc.nx = d[0];
+    sc.ny = d[1];
+    sc.nz = d[2];
+    sc.by = bits_for(sc.ny);
+    sc.bz = bits_for(sc.nz);
+    const int64_t nk = ((int64_t)sc.nx << (sc.by + sc.bz)) + 1;
+    if (nk > (int64_t)1 << 30) throw Error(SPH_ERR_CAPACITY, "uniform grid too large (raise cell_mult or shrink the box)");
+    sc.nkeys = (int)nk;
+    sc.k_cap = (int)round_up(nk, kChunk);
+    sc.nchunks = sc.k_cap / kChunk;
+    sc.tab_len = sc.ny + sc.nz;
+    sc.reach = (int)std::ceil(1.0 / (double)p.cell_mult - 1e-9);
+}
+
+void System::fill_dev(Scene& sc) {
+    const sph_params& p = sc.prm;
+    SceneDev& d = sc.dev;
+    std::memset(&d, 0, sizeof d);
+    d.p_off = (int)sc.p_off;
+    d.n = sc.n;
+    d.p_cap = sc.p_cap;
+    d.k_off = (int)sc.k_off;
+    d.nkeys = sc.nkeys;
+    d.k_cap = sc.k_cap;
+    d.c_off = (int)sc.c_off;
+    d.nchunks = sc.nchunks;
+    d.t_off = (int)sc.t_off;
+    d.tw = sc.tw;
+    d.td = sc.td;
+    d.tab_off = (int)sc.tab_off;
+    d.nx = sc.nx;
+    d.ny = sc.ny;
+    d.nz = sc.nz;
+    d.reach = sc.reach;
+    d.flags = 0;
+    if (sc.tw > 0) d.flags |= kFlagTerrain;
+    if (sc.tw > 0 && p.erosion) d.flags |= kFlagErosion;
+    if (p.flags & SPH_FLAG_RECORD) d.flags |= kFlagRecord;
+    if (p.flags & SPH_FLAG_ORDERED) d.flags |= kFlagOrdered;
+    for (int a = 0; a < 3; ++a) d.lo[a] = sc.lo[a];
+    d.inv_cell = sc.inv_cell;
+    // kernel constants, same FP32 expressions as fluid_system.h:415-452
+    // with PI = 3.141592f (Erosion/sphere.h:8)
+    const float h = p.smoothing_radius;
+    const float PI = 3.141592f;
+    d.h = h;
+    d.hh = h * h;
+    d.smax = smax_for(h);
+    d.cthr = coincidence_threshold();
+    d.mass = p.mass;
+    d.p0 = p.rest_density;
+    d.k = p.gas_stiffness;
+    d.visc = p.viscosity;
+    d.sigma = p.surface_tension;
+    d.dt = p.dt;
+    d.cr = p.restitution;
+    for (int a = 0; a < 3; ++a) d.g[a] = p.gravity[a];
+    d.c_poly6 = 315.0f / (64.0f * PI * powf(h, 9.0f));
+    d.c_grad = 945.0f / (32.0f * PI * powf(h, 9.0f));
+    d.c_spiky = 45.0f / (PI * powf(h, 6.0f));
+    {
+        const float three = (1.0f * 1.0f + 1.0f * 1.0f) + 1.0f * 1.0f;
+        d.inv_sqrt3 = 1.0f / sqrtf(three);
+    }
+    const bool iso = p.box_half[0] == p.box_half[1] && p.box_half[1] == p.box_half[2];
+    for (int a = 0; a < 3; ++a) {
+        d.box_c[a] = p.box_center[a];
+        d.box_l[a] = p.box_half[a];
+        d.box_w[a] = iso ? 1.0f : 1.0f / p.box_half[a];
+    }
+    if (sc.tw > 0) {
+        const float sx = (p.box_half[0] + p.box_half[0]) / (float)(sc.tw - 1);
+        const float sz = (p.box_half[2] + p.box_half[2]) / (float)(sc.td - 1);
+        d.t_xlo = p.box_center[0] - p.box_half[0];
+        d.t_ylo = p.box_center[1] - p.box_half[1];
+        d.t_zlo = p.box_center[2] - p.box_half[2];
+        d.t_isx = 1.0f / sx;
+        d.t_isz = 1.0f / sz;
+        d.t_wmax = (float)(sc.tw - 1);
+        d.t_dmax = (float)(sc.td - 1);
+        // one sediment unit = 2^-30 of a particle's rest volume, spread over
+        // the area of one vertex cell
+        d.height_unit = (float)(((double)p.mass / (double)p.rest_density) * std::ldexp(1.0, -30) /
+                                ((double)sx * (double)sz));
+    }
+    d.k_capacity = p.k_capacity;
+    d.k_pick = p.k_pickup;
+    d.k_dep = p.k_deposit;
+    d.layer = p.erosion_layer;
+}
+
+void System::upload_scene(int id) {
+    Scene& sc = scenes_[id];
+    fill_dev(sc);
+    SPH_CK(cudaMemcpyAsync(dscenes_.p + id, &sc.dev, sizeof(SceneDev), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemcpyAsync(steps_.p + id, &sc.steps, sizeof(int), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+}
+
+static void validate(const sph_params& p) {
+    if (!(p.smoothing_radius > 0.0f) || !std::isfinite(p.smoothing_radius))
+        throw Error(SPH_ERR_INVALID, "smoothing_radius must be positive");
+    for (int a = 0; a < 3; ++a)
+        if (!(p.box_half[a] > 0.0f) || !std::isfinite(p.box_half[a]))
+            throw Error(SPH_ERR_INVALID, "box_half must be positive");
+    if (!(p.cell_mult >= 0.5f) || !(p.cell_mult <= 8.0f)) throw Error(SPH_ERR_INVALID, "cell_mult must be in [0.5, 8]");
+}
+
+int System::create_scene(const sph_params& p, int capacity, int tw, int td) {
+    validate(p);
+    if (capacity < 0 || tw < 0 || td < 0) throw Error(SPH_ERR_INVALID, "negative size");
+    if ((tw > 0) != (td > 0) || (tw > 0 && (tw < 2 || td < 2)))
+        throw Error(SPH_ERR_INVALID, "terrain needs at least 2 x 2 vertices");
+    int id = -1;
+    for (int i = 0; i < (int)scenes_.size(); ++i)
+        if (!scenes_[i].live) {
+            id = i;
+            break;
+        }
+    if (id < 0) {
+        if ((int)scenes_.size() >= cfg_.max_scenes) throw Error(SPH_ERR_CAPACITY, "max_scenes reached");
+        scenes_.emplace_back();
+        id = (int)scenes_.size() - 1;
+    }
+    Scene sc;
+    sc.prm = p;
+    geometry(sc);
+    sc.p_cap = (int)round_up(std::max(capacity, 1), kPAlign);
+    sc.tw = tw;
+    sc.td = td;
+    check_budget(scene_bytes(sc.p_cap, tw, td, p));
+    ensure_arena(pa_, sc.p_cap, 0);
+    ensure_arena(ka_, sc.k_cap, 1);
+    ensure_arena(ca_, sc.nchunks, 2);
+    ensure_arena(tba_, sc.tab_len, 3);
+    const int64_t tlen = tw > 0 ? round_up((int64_t)tw * td, kTAlign) : 0;
+    if (tlen) ensure_arena(ta_, tlen, 4);
+    if (!pa_.alloc(sc.p_cap, &sc.p_off) || !ka_.alloc(sc.k_cap, &sc.k_off) || !ca_.alloc(sc.nchunks, &sc.c_off) ||
+        !tba_.alloc(sc.tab_len, &sc.tab_off) || (tlen && !ta_.alloc(tlen, &sc.t_off)))
+        throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+    if (p.flags & SPH_FLAG_RECORD && rec_.n == 0) {
+        rec_.resize(pos_.n * kRecFloats, false, st_);
+        drop_graph();
+    }
+    // interleave tables and clean key ranges
+    std::vector<uint32_t> tab(sc.tab_len);
+    for (int y = 0; y < sc.ny; ++y) tab[y] = yz_interleave(y, 0, sc.by, sc.bz);
+    for (int z = 0; z < sc.nz; ++z) tab[sc.ny + z] = yz_interleave(0, z, sc.by, sc.bz);
+    SPH_CK(cudaMemcpyAsync(tab_.p + sc.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemsetAsync(counts_.p + sc.k_off, 0, (size_t)sc.k_cap * 4, st_));
+    SPH_CK(cudaMemsetAsync(chunk_.p + sc.c_off, 0, (size_t)sc.nchunks * 4, st_));
+    if (tlen) {
+        SPH_CK(cudaMemsetAsync(tbase_.p + sc.t_off, 0, (size_t)tlen * 4, st_));
+        SPH_CK(cudaMemsetAsync(theight_.p + sc.t_off, 0, (size_t)tlen * 4, st_));
+        SPH_CK(cudaMemsetAsync(tdelta_.p + sc.t_off, 0, (size_t)tlen * 8, st_));
+    }
+    sc.live = true;
+    scenes_[id] = sc;
+    upload_scene(id);
+    work_dirty_ = true;
+    return id;
+}
+
+void System::destroy_scene(int id) {
+    Scene& sc = scene(id);
+    SPH_CK(cudaStreamSynchronize(st_));
+    pa_.release(sc.p_off, sc.p_cap);
+    ka_.release(sc.k_off, sc.k_cap);
+    ca_.release(sc.c_off, sc.nchunks);
+    tba_.release(sc.tab_off, sc.tab_len);
+    if (sc.tw > 0) ta_.release(sc.t_off, round_up((int64_t)sc.tw * sc.td, kTAlign));
+    sc.live = false;
+    sc.n = 0;
+    sc.steps = 0;
+    int zero = 0;
+    SPH_CK(cudaMemcpyAsync(steps_.p + id, &zero, sizeof(int), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    work_dirty_ = true;
+}
+
+void System::set_params(int id, const sph_params& p) {
+    validate(p);
+    Scene& sc = scene(id);
+    Scene ng = sc;
+    ng.prm = p;
+    geometry(ng);
+    if (ng.k_cap != sc.k_cap || ng.nchunks != sc.nchunks || ng.tab_len != sc.tab_len) {
+        SPH_CK(cudaStreamSynchronize(st_));
+        ka_.release(sc.k_off, sc.k_cap);
+        ca_.release(sc.c_off, sc.nchunks);
+        tba_.release(sc.tab_off, sc.tab_len);
+        ensure_arena(ka_, ng.k_cap, 1);
+        ensure_arena(ca_, ng.nchunks, 2);
+        ensure_arena(tba_, ng.tab_len, 3);
+        if (!ka_.alloc(ng.k_cap, &ng.k_off) || !ca_.alloc(ng.nchunks, &ng.c_off) || !tba_.alloc(ng.tab_len, &ng.tab_off))
+            throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+        SPH_CK(cudaMemsetAsync(counts_.p + ng.k_off, 0, (size_t)ng.k_cap * 4, st_));
+        SPH_CK(cudaMemsetAsync(chunk_.p + ng.c_off, 0, (size_t)ng.nchunks * 4, st_));
+        work_dirty_ = true;
+    }
+    if (ng.nx != sc.nx || ng.ny != sc.ny || ng.nz != sc.nz || ng.tab_off != sc.tab_off) {
+        std::vector<uint32_t> tab(ng.tab_len);
+        for (int y = 0; y < ng.ny; ++y) tab[y] = yz_interleave(y, 0, ng.by, ng.bz);
+        for (int z = 0; z < ng.nz; ++z) tab[ng.ny + z] = yz_interleave(0, z, ng.by, ng.bz);
+        SPH_CK(cudaMemcpyAsync(tab_.p + ng.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
+    }
+    if ((p.flags & SPH_FLAG_RECORD) && rec_.n == 0) {
+        SPH_CK(cudaStreamSynchronize(st_));
+        rec_.resize(pos_.n * kRecFloats, false, st_);
+        drop_graph();
+    }
+    if ((p.flags ^ sc.prm.flags) & (SPH_FLAG_ORDERED | SPH_FLAG_RECORD)) work_dirty_ = true;
+    sc = ng;
+    upload_scene(id);
+}
+
+void System::set_steps(int id, int steps) {
+    Scene& sc = scene(id);
+    sc.steps = steps < 0 ? -1 : steps;
+    SPH_CK(cudaMemcpyAsync(steps_.p + id, &sc.steps, sizeof(int), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    work_dirty_ = true;
+}
+
+void System::ensure_particle_cap(Scene& sc, int need) {
+    if (need <= sc.p_cap) return;
+    const int ncap = (int)round_up(std::max<int64_t>(need, (int64_t)sc.p_cap * 2), kPAlign);
+    SPH_CK(cudaStreamSynchronize(st_));
+    ensure_arena(pa_, ncap, 0);
+    int64_t noff;
+    if (!pa_.alloc(ncap, &noff)) throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+    if (sc.n > 0) {
+        SPH_CK(cudaMemcpyAsync(pos_.p + noff, pos_.p + sc.p_off, (size_t)sc.n * 16, cudaMemcpyDeviceToDevice, st_));
+        SPH_CK(cudaMemcpyAsync(vel_.p + noff, vel_.p + sc.p_off, (size_t)sc.n * 16, cudaMemcpyDeviceToDevice, st_));
+        SPH_CK(cudaMemcpyAsync(nbid_.p + noff, nbid_.p + sc.p_off, (size_t)sc.n * 4, cudaMemcpyDeviceToDevice, st_));
+        SPH_CK(cudaMemcpyAsync(dyn_.p + noff, dyn_.p + sc.p_off, (size_t)sc.n * 16, cudaMemcpyDeviceToDevice, st_));
+        SPH_CK(cudaStreamSynchronize(st_));
+    }
+    pa_.release(sc.p_off, sc.p_cap);
+    sc.p_off = noff;
+    sc.p_cap = ncap;
+    work_dirty_ = true;
+}
+
+void System::set_particles(int id, int n, const float* pos3, const float* vel3) {
+    if (n < 0 || (n > 0 && !pos3)) throw Error(SPH_ERR_INVALID, "bad particle arrays");
+    Scene& sc = scene(id);
+    SPH_CK(cudaStreamSynchronize(st_));
+    ensure_particle_cap(sc, n);
+    std::vector<float4> hp(n), hv(n);
+    std::vector<int32_t> nb(n, -1);
+    for (int i = 0; i < n; ++i) {
+        hp[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], bits_to_float(i));
+        hv[i] = vel3 ? make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], bits_to_float(0))
+                     : make_float4(0.f, 0.f, 0.f, bits_to_float(0));
+    }
+    if (n > 0) {
+        SPH_CK(cudaMemcpyAsync(pos_.p + sc.p_off, hp.data(), (size_t)n * 16, cudaMemcpyHostToDevice, st_));
+        SPH_CK(cudaMemcpyAsync(vel_.p + sc.p_off, hv.data(), (size_t)n * 16, cudaMemcpyHostToDevice, st_));
+        SPH_CK(cudaMemcpyAsync(nbid_.p + sc.p_off, nb.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st_));
+        SPH_CK(cudaMemsetAsync(dyn_.p + sc.p_off, 0, (size_t)n * 16, st_));
+    }
+    SPH_CK(cudaStreamSynchronize(st_));
+    if (sc.n != n) work_dirty_ = true;
+    sc.n = n;
+    upload_scene(id);
+}
+
+// Initialize(n) / AddParticles(n) (fluid_system.h:74-102, :232-251): a lattice
+// of ceil(cbrt(n))^3 particles at spacing 0.025 from (-0.2,-0.05,-0.15) plus
+// the origin, appended after the existing particles with the next ids.
+int System::add_lattice(int id, int n, const float origin[3]) {
+    if (n < 0) throw Error(SPH_ERR_INVALID, "negative count");
+    Scene& sc = scene(id);
+    std::vector<float4> hp, hv;
+    const double cn = std::cbrt((double)n);
+    int next = sc.n;
+    for (int i = 0; i < cn; i++)
+        for (int j = 0; j < cn; j++)
+            for (int k = 0; k < cn; k++) {
+                const float x = -0.2 + i * 0.025;
+                const float y = -0.05 + j * 0.025;
+                const float z = -0.15 + k * 0.025;
+                hp.push_back(make_float4(x + origin[0], y + origin[1], z + origin[2], bits_to_float(next++)));
+                hv.push_back(make_float4(0.f, 0.f, 0.f, bits_to_float(0)));
+            }
+    const int add = (int)hp.size();
+    if (add == 0) return 0;
+    SPH_CK(cudaStreamSynchronize(st_));
+    ensure_particle_cap(sc, sc.n + add);
+    std::vector<int32_t> nb(add, -1);
+    SPH_CK(cudaMemcpyAsync(pos_.p + sc.p_off + sc.n, hp.data(), (size_t)add * 16, cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemcpyAsync(vel_.p + sc.p_off + sc.n, hv.data(), (size_t)add * 16, cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemcpyAsync(nbid_.p + sc.p_off + sc.n, nb.data(), (size_t)add * 4, cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemsetAsync(dyn_.p + sc.p_off + sc.n, 0, (size_t)add * 16, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    sc.n += add;
+    work_dirty_ = true;
+    upload_scene(id);
+    return add;
+}
+
+void System::get_particles(int id, float* pos3, float* vel3, float* density, int32_t* sed) {
+    Scene& sc = scene(id);
+    SPH_CK(cudaStreamSynchronize(st_));
+    check_status();
+    const int n = sc.n;
+    std::vector<float4> hp(n), hv(n), hd;
+    if (n == 0) return;
+    SPH_CK(cudaMemcpyAsync(hp.data(), pos_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(hv.data(), vel_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    if (density) {
+        hd.resize(n);
+        SPH_CK(cudaMemcpyAsync(hd.data(), dyn_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    }
+    SPH_CK(cudaStreamSynchronize(st_));
+    for (int p = 0; p < n; ++p) {
+        const int i = float_to_bits(hp[p].w);
+        if (i < 0 || i >= n) throw Error(SPH_ERR_DEVICE, "corrupt particle id");
+        if (pos3) {
+            pos3[3 * i] = hp[p].x;
+            pos3[3 * i + 1] = hp[p].y;
+            pos3[3 * i + 2] = hp[p].z;
+        }
+        if (vel3) {
+            vel3[3 * i] = hv[p].x;
+            vel3[3 * i + 1] = hv[p].y;
+            vel3[3 * i + 2] = hv[p].z;
+        }
+        if (density) density[i] = hd[p].x;
+        if (sed) sed[i] = float_to_bits(hv[p].w);
+    }
+}
+
+void System::get_records(int id, float* rec27, int* nbid, int32_t* sed) {
+    Scene& sc = scene(id);
+    SPH_CK(cudaStreamSynchronize(st_));
+    check_status();
+    const int n = sc.n;
+    if (n == 0) return;
+    std::vector<float4> hp(n), hv(n), hd(n);
+    std::vector<float> hr;
+    std::vector<int32_t> hn(n);
+    SPH_CK(cudaMemcpyAsync(hp.data(), pos_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(hv.data(), vel_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(hd.data(), dyn_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(hn.data(), nbid_.p + sc.p_off, (size_t)n * 4, cudaMemcpyDeviceToHost, st_));
+    const bool have_rec = (sc.prm.flags & SPH_FLAG_RECORD) && rec_.n > 0;
+    if (have_rec) {
+        hr.resize((size_t)n * kRecFloats);
+        SPH_CK(cudaMemcpyAsync(hr.data(), rec_.p + (size_t)sc.p_off * kRecFloats, hr.size() * 4,
+                               cudaMemcpyDeviceToHost, st_));
+    }
+    SPH_CK(cudaStreamSynchronize(st_));
+    for (int p = 0; p < n; ++p) {
+        const int i = float_to_bits(hp[p].w);
+        if (i < 0 || i >= n) throw Error(SPH_ERR_DEVICE, "corrupt particle id");
+        if (rec27) {
+            float* r = rec27 + (size_t)27 * i;
+            r[0] = hp[p].x; r[1] = hp[p].y; r[2] = hp[p].z;
+            r[3] = hv[p].x; r[4] = hv[p].y; r[5] = hv[p].z;
+            r[9] = hd[p].x;
+            r[10] = hd[p].w;
+            for (int q = 0; q < kRecFloats; ++q) {
+                const int dst = q < 3 ? 6 + q : 8 + q;  // acc -> 6..8, forces/normal -> 11..25
+                r[dst] = have_rec ? hr[(size_t)p * kRecFloats + q] : 0.0f;
+            }
+            r[26] = 0.0f;
+        }
+        if (nbid) nbid[i] = hn[p];
+        if (sed) sed[i] = float_to_bits(hv[p].w);
+    }
+}
+
+void System::diag(int id, sph_diag* out) {
+    Scene& sc = scene(id);
+    if (work_dirty_) rebuild_work();
+    SPH_CK(cudaMemcpyAsync(slist_.p, &id, sizeof(int), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemsetAsync(diag_i_.p, 0, 2 * sizeof(long long), st_));
+    SPH_CK(cudaMemsetAsync(diag_nan_.p, 0, sizeof(int), st_));
+    launch_diag(arrays(), 1, diag_part_.p, diag_i_.p, diag_nan_.p, st_);
+    SPH_CK(cudaGetLastError());
+    std::vector<double> part((size_t)kDiagBlocks * kDiagDoubles);
+    long long is[2];
+    int nan = 0;
+    SPH_CK(cudaMemcpyAsync(part.data(), diag_part_.p, part.size() * 8, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(is, diag_i_.p, sizeof is, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(&nan, diag_nan_.p, sizeof nan, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    double acc[kDiagDoubles] = {0};
+    for (int b = 0; b < kDiagBlocks; ++b)
+        for (int c = 0; c < kDiagDoubles; ++c) acc[c] += part[(size_t)b * kDiagDoubles + c];
+    std::memset(out, 0, sizeof *out);
+    out->fluid_mass = (double)sc.n * (double)sc.prm.mass;
+    out->momentum[0] = acc[0];
+    out->momentum[1] = acc[1];
+    out->momentum[2] = acc[2];
+    out->kinetic = acc[3];
+    out->potential = acc[4];
+    out->sediment_units = is[0];
+    out->terrain_units = is[1];
+    out->total_units = is[0] + is[1];
+    out->unit_volume = ((double)sc.prm.mass / (double)sc.prm.rest_density) * std::ldexp(1.0, -30);
+    out->n = sc.n;
+    out->nan_particles = nan;
+}
+
+void System::upload_terrain_height(Scene& sc) {
+    // snapshot = base + delta * unit with delta = 0
+    SPH_CK(cudaMemcpyAsync(theight_.p + sc.t_off, tbase_.p + sc.t_off, (size_t)sc.tw * sc.td * 4,
+                           cudaMemcpyDeviceToDevice, st_));
+}
+
+void System::set_terrain(int id, int w, int d, const float* heights) {
+    if (w < 2 || d < 2 || !heights) throw Error(SPH_ERR_INVALID, "terrain needs at least 2 x 2 heights");
+    Scene& sc = scene(id);
+    SPH_CK(cudaStreamSynchronize(st_));
+    if (w != sc.tw || d != sc.td) {
+        if (sc.tw > 0) ta_.release(sc.t_off, round_up((int64_t)sc.tw * sc.td, kTAlign));
+        const int64_t tlen = round_up((int64_t)w * d, kTAlign);
+        ensure_arena(ta_, tlen, 4);
+        if (!ta_.alloc(tlen, &sc.t_off)) throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+        sc.tw = w;
+        sc.td = d;
+        work_dirty_ = true;
+    }
+    SPH_CK(cudaMemcpyAsync(tbase_.p + sc.t_off, heights, (size_t)w * d * 4, cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemsetAsync(tdelta_.p + sc.t_off, 0, (size_t)w * d * 8, st_));
+    upload_terrain_height(sc);
+    SPH_CK(cudaStreamSynchronize(st_));
+    upload_scene(id);
+    work_dirty_ = true;
+}
+
+void System::gen_terrain(int id, uint64_t seed, int octaves, float amp, float lac, float gain, int kind) {
+    Scene& sc = scene(id);
+    if (sc.tw < 2) throw Error(SPH_ERR_STATE, "scene has no terrain grid");
+    std::vector<float> h((size_t)sc.tw * sc.td);
+    fbm_heights(seed, sc.tw, sc.td, octaves, amp, lac, gain, kind, h.data());
+    set_terrain(id, sc.tw, sc.td, h.data());
+}
+
+void System::get_terrain(int id, float* heights, int64_t* delta) {
+    Scene& sc = scene(id);
+    if (sc.tw < 2) throw Error(SPH_ERR_STATE, "scene has no terrain");
+    SPH_CK(cudaStreamSynchronize(st_));
+    const size_t nt = (size_t)sc.tw * sc.td;
+    if (heights) SPH_CK(cudaMemcpyAsync(heights, theight_.p + sc.t_off, nt * 4, cudaMemcpyDeviceToHost, st_));
+    if (delta) SPH_CK(cudaMemcpyAsync(delta, tdelta_.p + sc.t_off, nt * 8, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+}
+
+void System::terrain_dims(int id, int* w, int* d) const {
+    const Scene& sc = scene(id);
+    *w = sc.tw;
+    *d = sc.td;
+}
+
+void System::grid_dims(int id, int* dims4) const {
+    const Scene& sc = scene(id);
+    dims4[0] = sc.nx;
+    dims4[1] = sc.ny;
+    dims4[2] = sc.nz;
+    dims4[3] = sc.nkeys;
+}
+
+// ---- work lists and launches -------------------------------------------------
+void System::rebuild_work() {
+    std::vector<Work> pt, ct, tt;
+    any_fast_ = any_ordered_ = any_terrain_ = any_limited_ = any_record_ = false;
+    const int tile = cfg_.tile;
+    for (int id = 0; id < (int)scenes_.size(); ++id) {
+        const Scene& sc = scenes_[id];
+        if (!sc.live || sc.n == 0) continue;
+        for (int t = 0; t * tile < sc.n; ++t) pt.push_back({id, (int)sc.p_off + t * tile});
+        for (int c = 0; c < sc.nchunks; ++c) ct.push_back({id, c});
+        if (sc.tw > 0)
+            for (int64_t t = 0; t * tile < (int64_t)sc.tw * sc.td; ++t) tt.push_back({id, (int)(sc.t_off + t * tile)});
+        if (sc.prm.flags & SPH_FLAG_ORDERED)
+            any_ordered_ = true;
+        else
+            any_fast_ = true;
+        if (sc.tw > 0) any_terrain_ = true;
+        if (sc.prm.flags & SPH_FLAG_RECORD) any_record_ = true;
+    }
+    for (const Scene& sc : scenes_)
+        if (sc.live && sc.steps >= 0) any_limited_ = true;
+    auto up = [&](DevBuf<Work>& b, const std::vector<Work>& v) {
+        if ((int64_t)v.size() > b.n) {
+            b.resize(std::max<int64_t>((int64_t)v.size(), b.n * 2), false, st_);
+            drop_graph();
+        }
+        if (!v.empty())
+            SPH_CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(Work), cudaMemcpyHostToDevice, st_));
+    };
+    up(ptiles_, pt);
+    up(ctiles_, ct);
+    up(ttiles_, tt);
+    int counts[4] = {(int)pt.size(), (int)ct.size(), (int)tt.size(), 0};
+    SPH_CK(cudaMemcpyAsync(nwork_.p, counts, sizeof counts, cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    if (n_ptiles_ != counts[0] || n_ctiles_ != counts[1] || n_ttiles_ != counts[2]) drop_graph();
+    n_ptiles_ = counts[0];
+    n_ctiles_ = counts[1];
+    n_ttiles_ = counts[2];
+    work_dirty_ = false;
+    drop_graph();
+}
+
+DevArrays System::arrays() const {
+    DevArrays a;
+    a.scenes = dscenes_.p;
+    a.steps_left = steps_.p;
+    a.ptiles = ptiles_.p;
+    a.n_ptiles = nwork_.p;
+    a.ctiles = ctiles_.p;
+    a.n_ctiles = nwork_.p + 1;
+    a.ttiles = ttiles_.p;
+    a.n_ttiles = nwork_.p + 2;
+    a.scene_list = slist_.p;
+    a.pos = pos_.p;
+    a.vel = vel_.p;
+    a.spos = spos_.p;
+    a.svel = svel_.p;
+    a.dyn = dyn_.p;
+    a.key = key_.p;
+    a.slot = slot_.p;
+    a.perm = perm_.p;
+    a.nbid = nbid_.p;
+    a.snbid = snbid_.p;
+    a.rec = rec_.p;
+    a.counts = counts_.p;
+    a.offsets = offsets_.p;
+    a.chunk_sum = chunk_.p;
+    a.tab = tab_.p;
+    a.tbase = tbase_.p;
+    a.tdelta = tdelta_.p;
+    a.theight = theight_.p;
+    a.status = status_.p;
+    return a;
+}
+
+LaunchShape System::shape() const {
+    LaunchShape s;
+    s.tile = cfg_.tile;
+    s.grid_p = n_ptiles_;
+    s.grid_c = n_ctiles_;
+    s.grid_t = n_ttiles_;
+    return s;
+}
+
+void System::enqueue_sort(const DevArrays& a, const LaunchShape& s) {
+    launch_keys(a, s, st_);
+    launch_scan(a, s, st_);
+    launch_scatter(a, s, st_);
+    launch_reorder(a, s, st_);
+}
+
+void System::enqueue_step(const DevArrays& a, const LaunchShape& s, cudaEvent_t* ev) {
+    auto mark = [&](int i) {
+        if (ev) SPH_CK(cudaEventRecord(ev[i], st_));
+    };
+    mark(0);
+    launch_keys(a, s, st_);
+    mark(1);
+    launch_scan(a, s, st_);
+    mark(2);
+    launch_scatter(a, s, st_);
+    mark(3);
+    launch_reorder(a, s, st_);
+    mark(4);
+    if (any_fast_) launch_density(a, s, st_);
+    if (any_ordered_) launch_density_ordered(a, s, st_);
+    mark(5);
+    if (any_fast_) launch_force(a, s, st_);
+    if (any_ordered_) launch_force_ordered(a, s, st_);
+    mark(6);
+    if (any_terrain_ && s.grid_t > 0) launch_terrain(a, s, st_);
+    mark(7);
+    if (any_limited_) launch_tick(a, (int)scenes_.size(), st_);
+    mark(8);
+}
+
+void System::capture_graph() {
+    drop_graph();
+    const DevArrays a = arrays();
+    const LaunchShape s = shape();
+    SPH_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < cfg_.graph_steps; ++i) enqueue_step(a, s, nullptr);
+    cudaGraph_t g = nullptr;
+    SPH_CK(cudaStreamEndCapture(st_, &g));
+    graph_ = g;
+    SPH_CK(cudaGraphInstantiate(&gexec_, graph_, 0));
+    graph_dirty_ = false;
+}
+
+void System::step(int nsteps) {
+    if (nsteps < 0) throw Error(SPH_ERR_INVALID, "negative step count");
+    if (work_dirty_) rebuild_work();
+    if (n_ptiles_ > 0 && nsteps > 0) {
+        const DevArrays a = arrays();
+        const LaunchShape s = shape();
+        int done = 0;
+        const int g = cfg_.graph_steps;
+        if (g > 0 && nsteps >= g) {
+            if (graph_dirty_ || !gexec_) capture_graph();
+            while (nsteps - done >= g) {
+                SPH_CK(cudaGraphLaunch(gexec_, st_));
+                done += g;
+            }
+        }
+        for (; done < nsteps; ++done) enqueue_step(a, s, nullptr);
+        SPH_CK(cudaGetLastError());
+        advance_step_mirror(nsteps);
+    }
+}
+
+// Host copy of the per-scene step budgets, decremented like k_tick does.
+void System::advance_step_mirror(int nsteps) {
+    if (!any_limited_) return;
+    for (Scene& sc : scenes_)
+        if (sc.live && sc.steps > 0) sc.steps = std::max(0, sc.steps - nsteps);
+}
+
+void System::sync() {
+    SPH_CK(cudaStreamSynchronize(st_));
+    check_status();
+}
+
+// Kernel-reported conditions (ordered-mode neighbour overflow) become an
+// error of the next host call that reads results.
+void System::check_status() {
+    const unsigned v = read_status();
+    if (v == 0) return;
+    const unsigned zero = 0;
+    SPH_CK(cudaMemcpyAsync(status_.p, &zero, sizeof zero, cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    if (v & 1u)
+        throw Error(SPH_ERR_DEVICE, "ordered mode: a particle had more in-range neighbours than the list holds");
+    if (v & 2u) throw Error(SPH_ERR_DEVICE, "counting sort found inconsistent cell counts");
+    throw Error(SPH_ERR_DEVICE, "kernel status " + std::to_string(v));
+}
+
+float System::time_steps(int nsteps) {
+    if (work_dirty_) rebuild_work();
+    if (cfg_.graph_steps > 0 && nsteps >= cfg_.graph_steps && (graph_dirty_ || !gexec_) && n_ptiles_ > 0)
+        capture_graph();
+    cudaEvent_t e0, e1;
+    SPH_CK(cudaEventCreate(&e0));
+    SPH_CK(cudaEventCreate(&e1));
+    SPH_CK(cudaEventRecord(e0, st_));
+    step(nsteps);
+    SPH_CK(cudaEventRecord(e1, st_));
+    SPH_CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    SPH_CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms;
+}
+
+void System::profile_stages(int nsteps, float* ms) {
+    if (work_dirty_) rebuild_work();
+    for (int i = 0; i < 8; ++i) ms[i] = 0.f;
+    if (n_ptiles_ == 0 || nsteps <= 0) return;
+    cudaEvent_t ev[9];
+    for (auto& e : ev) SPH_CK(cudaEventCreate(&e));
+    const DevArrays a = arrays();
+    const LaunchShape s = shape();
+    for (int k = 0; k < nsteps; ++k) {
+        enqueue_step(a, s, ev);
+        SPH_CK(cudaEventSynchronize(ev[8]));
+        for (int i = 0; i < 8; ++i) {
+            float t = 0.f;
+            SPH_CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+            ms[i] += t;
+        }
+    }
+    for (int i = 0; i < 8; ++i) ms[i] /= (float)nsteps;
+    for (auto& e : ev) cudaEventDestroy(e);
+    advance_step_mirror(nsteps);
+}
+
+unsigned System::read_status() {
+    unsigned v = 0;
+    SPH_CK(cudaMemcpyAsync(&v, status_.p, sizeof v, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    return v;
+}
+
+void System::debug_sort(int id, uint32_t* keys_by_id, int32_t* sorted_ids) {
+    Scene& sc = scene(id);
+    if (work_dirty_) rebuild_work();
+    if (sc.n == 0) return;
+    enqueue_sort(arrays(), shape());
+    SPH_CK(cudaGetLastError());
+    const int n = sc.n;
+    std::vector<float4> hp(n), hs(n);
+    std::vector<uint32_t> hk(n);
+    SPH_CK(cudaMemcpyAsync(hp.data(), pos_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(hs.data(), spos_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(hk.data(), key_.p + sc.p_off, (size_t)n * 4, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    for (int i = 0; i < n; ++i) {
+        const int pid = float_to_bits(hp[i].w);
+        if (keys_by_id) keys_by_id[pid] = hk[i];
+        if (sorted_ids) sorted_ids[i] = float_to_bits(hs[i].w);
+    }
+}
+
+void System::neighbour_counts(int id, int32_t* out) {
+    Scene& sc = scene(id);
+    if (work_dirty_) rebuild_work();
+    if (sc.n == 0) return;
+    if (scratch_i_.n < pos_.n) scratch_i_.resize(pos_.n, false, st_);
+    const DevArrays a = arrays();
+    enqueue_sort(a, shape());
+    launch_neighbour_counts(a, shape(), scratch_i_.p, st_);
+    SPH_CK(cudaGetLastError());
+    SPH_CK(cudaMemcpyAsync(out, scratch_i_.p + sc.p_off, (size_t)sc.n * 4, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+}
+
+template struct DevBuf<float4>;
+template struct DevBuf<float>;
+template struct DevBuf<uint32_t>;
+template struct DevBuf<int32_t>;
+template struct DevBuf<long long>;
+template struct DevBuf<double>;
+template struct DevBuf<SceneDev>;
+template struct DevBuf<Work>;
+
+}  // namespace sph

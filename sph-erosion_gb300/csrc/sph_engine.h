@@ -1,0 +1,179 @@
+// Host engine of the simulation step: device arenas, scenes, work lists,
+// step orchestration and CUDA-graph capture.  Internal to libsph_gb300.so;
+// the public surface is include/sph_erosion.h.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sph_erosion.h"
+#include "sph_kernels.h"
+#include "sph_types.h"
+
+namespace sph {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void check_cuda(cudaError_t e, const char* what);
+#define SPH_CK(x) ::sph::check_cuda((x), #x)
+
+// First-fit allocator of index ranges inside one arena.
+class RangeAlloc {
+   public:
+    void reset(int64_t cap);
+    bool alloc(int64_t len, int64_t* off);  // len already rounded by the caller
+    void release(int64_t off, int64_t len);
+    void grow(int64_t cap);
+    int64_t cap() const { return cap_; }
+    int64_t used() const { return used_; }
+
+   private:
+    std::map<int64_t, int64_t> free_;  // offset -> length
+    int64_t cap_ = 0;
+    int64_t used_ = 0;
+};
+
+// A typed device buffer that can grow while keeping its contents.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    int64_t n = 0;
+    void resize(int64_t cnt, bool keep, cudaStream_t st);
+    void release();
+    int64_t bytes() const { return n * (int64_t)sizeof(T); }
+};
+
+struct Scene {
+    bool live = false;
+    sph_params prm{};
+    int n = 0;
+    int p_cap = 0;
+    int64_t p_off = 0;
+    int nx = 1, ny = 1, nz = 1, by = 0, bz = 0, reach = 1;
+    int nkeys = 0, k_cap = 0, nchunks = 0;
+    int64_t k_off = 0, c_off = 0, tab_off = 0;
+    int tab_len = 0;
+    float cell = 0.f, inv_cell = 0.f, lo[3] = {0, 0, 0};
+    int tw = 0, td = 0;
+    int64_t t_off = 0;
+    int steps = -1;  // -1 unlimited, 0 inactive
+    SceneDev dev{};
+};
+
+class System {
+   public:
+    explicit System(const sph_system_config& cfg);
+    ~System();
+
+    int create_scene(const sph_params& p, int capacity, int tw, int td);
+    void destroy_scene(int id);
+    void set_params(int id, const sph_params& p);
+    const sph_params& params(int id) const { return scene(id).prm; }
+    void set_steps(int id, int steps);
+    int steps(int id) const { return scene(id).steps; }
+    void set_particles(int id, int n, const float* pos3, const float* vel3);
+    int add_lattice(int id, int n, const float origin[3]);
+    int count(int id) const { return scene(id).n; }
+    void get_particles(int id, float* pos3, float* vel3, float* density, int32_t* sed);
+    void get_records(int id, float* rec27, int* nbid, int32_t* sed);
+    void diag(int id, sph_diag* out);
+    void set_terrain(int id, int w, int d, const float* heights);
+    void gen_terrain(int id, uint64_t seed, int octaves, float amp, float lac, float gain, int kind);
+    void get_terrain(int id, float* heights, int64_t* delta);
+    void terrain_dims(int id, int* w, int* d) const;
+    void debug_sort(int id, uint32_t* keys_by_id, int32_t* sorted_ids);
+    void neighbour_counts(int id, int32_t* out);
+    void grid_dims(int id, int* dims4) const;
+
+    void step(int nsteps);
+    void sync();
+    float time_steps(int nsteps);
+    void profile_stages(int nsteps, float* ms);
+    int64_t memory_bytes() const;
+    int num_scenes() const { return (int)scenes_.size(); }
+    bool scene_live(int id) const { return id >= 0 && id < (int)scenes_.size() && scenes_[id].live; }
+    int64_t scene_bytes(int n, int tw, int td, const sph_params& p) const;
+    cudaStream_t stream() const { return st_; }
+    unsigned read_status();
+    void check_status();
+
+   private:
+    Scene& scene(int id);
+    const Scene& scene(int id) const;
+    void geometry(Scene& sc);
+    void fill_dev(Scene& sc);
+    void upload_scene(int id);
+    void ensure_particle_cap(Scene& sc, int need);
+    void ensure_arena(RangeAlloc& ra, int64_t need, int which);
+    void grow_particles(int64_t cap);
+    void grow_keys(int64_t cap);
+    void grow_terrain(int64_t cap);
+    void grow_tables(int64_t cap);
+    void grow_chunks(int64_t cap);
+    void rebuild_work();
+    DevArrays arrays() const;
+    LaunchShape shape() const;
+    void enqueue_step(const DevArrays& a, const LaunchShape& s, cudaEvent_t* ev);
+    void enqueue_sort(const DevArrays& a, const LaunchShape& s);
+    void capture_graph();
+    void advance_step_mirror(int nsteps);
+    void drop_graph();
+    void check_budget(int64_t extra) const;
+    void upload_terrain_height(Scene& sc);
+
+    sph_system_config cfg_;
+    int dev_ = 0, nsm_ = 1;
+    cudaStream_t st_ = nullptr;
+    std::vector<Scene> scenes_;
+
+    RangeAlloc pa_, ka_, ca_, ta_, tba_;
+    // particle arena
+    DevBuf<float4> pos_, vel_, spos_, svel_, dyn_;
+    DevBuf<uint32_t> key_, slot_, perm_;
+    DevBuf<int32_t> nbid_, snbid_;
+    DevBuf<float> rec_;
+    // key arena
+    DevBuf<uint32_t> counts_, offsets_;
+    DevBuf<uint32_t> chunk_;
+    DevBuf<uint32_t> tab_;
+    // terrain arena
+    DevBuf<float> tbase_, theight_;
+    DevBuf<long long> tdelta_;
+    // tables and work lists
+    DevBuf<SceneDev> dscenes_;
+    DevBuf<int> steps_;
+    DevBuf<Work> ptiles_, ctiles_, ttiles_;
+    DevBuf<int> nwork_;    // [0] particle tiles, [1] chunks, [2] terrain tiles
+    DevBuf<int> slist_;
+    DevBuf<unsigned> status_;
+    DevBuf<int32_t> scratch_i_;
+    DevBuf<double> diag_part_;
+    DevBuf<long long> diag_i_;
+    DevBuf<int> diag_nan_;
+
+    int n_ptiles_ = 0, n_ctiles_ = 0, n_ttiles_ = 0;
+    bool any_fast_ = false, any_ordered_ = false, any_terrain_ = false, any_limited_ = false,
+         any_record_ = false;
+    bool work_dirty_ = true;
+
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t gexec_ = nullptr;
+    bool graph_dirty_ = true;
+};
+
+// Host implementation of the seeded fBm generator (sph_terrain.cpp).
+void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, float lacunarity, float gain,
+                 int kind, float* out);
+
+// Host FP32 constants of a scene (sph_engine.cu): exposed for inspection.
+float smax_for(float h);
+float coincidence_threshold();
+
+}  // namespace sph

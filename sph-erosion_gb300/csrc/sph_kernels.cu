@@ -1,0 +1,706 @@
+// Hand-written sm_103a kernels of one simulation step, all scenes of a system
+// per launch.  Persistent grid-stride loops over a work list of tiles; a scene
+// whose step budget is exhausted is skipped.
+//
+// Stage order per step (the reference's Run, Erosion/fluid_system.h:104-183,
+// with its three O(N^2) passes replaced by a uniform grid):
+//   keys -> scan -> scatter -> reorder   counting sort into (y,z)-Morton rows
+//   density                               pass 1 (:107-124)
+//   force                                 passes 2 and 3 (:127-178), advance
+//                                         (:306-353), box (:355-407), terrain
+//                                         contact and erosion exchange
+//   terrain                               height snapshot for the next step
+//
+// Every arithmetic operation of the physics uses an explicitly rounded
+// intrinsic (__fmul_rn, __fadd_rn, ...), which the compiler never contracts
+// into a fused multiply-add, so each term rounds exactly like the reference's
+// scalar FP32 code.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sph_kernels.h"
+
+namespace sph {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsq(float a) { return __fsqrt_rn(a); }
+
+// x^2 with one rounding (what a correctly rounded powf(x, 2.0f) returns).
+__device__ __forceinline__ float pow2(float x) { return __fmul_rn(x, x); }
+
+// x^3 rounded once in all but near-tie cases: x*x = p + e exactly and
+// p*x = c + f exactly (TwoProduct with FMA; Ogita, Rump and Oishi, "Accurate
+// sum and dot product", SIAM J. Sci. Comput. 2005), then c + (f + e*x).
+__device__ __forceinline__ float pow3(float x) {
+    float p = __fmul_rn(x, x);
+    float e = __fmaf_rn(x, x, -p);
+    float c = __fmul_rn(p, x);
+    float f = __fmaf_rn(p, x, -c);
+    float t = __fmaf_rn(e, x, f);
+    return __fadd_rn(c, t);
+}
+
+// Squared distance of the reference's glm::length, (dx*dx + dy*dy) + dz*dz.
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return fa(fa(fm(dx, dx), fm(dy, dy)), fm(dz, dz));
+}
+
+__device__ __forceinline__ int cell_coord(float x, float lo, float inv, int n) {
+    float t = fm(fs(x, lo), inv);
+    if (!(t > 0.0f)) t = 0.0f;  // also maps NaN to 0
+    float top = (float)(n - 1);
+    if (t > top) t = top;
+    return (int)t;
+}
+
+struct Cell {
+    int cx, cy, cz;
+};
+
+__device__ __forceinline__ Cell cell_of(const SceneDev& S, float x, float y, float z) {
+    Cell c;
+    c.cx = cell_coord(x, S.lo[0], S.inv_cell, S.nx);
+    c.cy = cell_coord(y, S.lo[1], S.inv_cell, S.ny);
+    c.cz = cell_coord(z, S.lo[2], S.inv_cell, S.nz);
+    return c;
+}
+
+__device__ __forceinline__ uint32_t row_key(const uint32_t* tab, const SceneDev& S, int cy, int cz) {
+    return (__ldg(tab + S.tab_off + cy) | __ldg(tab + S.tab_off + S.ny + cz)) * (uint32_t)S.nx;
+}
+
+// Visit every particle in the (2R+1)^3 cells around c, cell rows merged
+// along x (x-adjacent cells of a row are contiguous in key order).  f(j, xj)
+// receives the scene-local sorted index and the position.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const DevArrays& a, const SceneDev& S, Cell c, F&& f) {
+    const int R = S.reach;
+    const uint32_t* off = a.offsets + S.k_off;
+    const float4* sp = a.spos + S.p_off;
+    const int xl = max(c.cx - R, 0), xh = min(c.cx + R, S.nx - 1);
+    for (int dz = -R; dz <= R; ++dz) {
+        const int z = c.cz + dz;
+        if (z < 0 || z >= S.nz) continue;
+        for (int dy = -R; dy <= R; ++dy) {
+            const int y = c.cy + dy;
+            if (y < 0 || y >= S.ny) continue;
+            const uint32_t row = row_key(a.tab, S, y, z);
+            const uint32_t st = __ldg(off + row + xl);
+            const uint32_t en = __ldg(off + row + xh + 1);
+            for (uint32_t j = st; j < en; ++j) f(j, __ldg(sp + j));
+        }
+    }
+}
+
+// Ordered (validation) traversal: collect in-range candidates, sort them by
+// particle id and visit them in ascending id, which is the reference's
+// summation order (all j ascending).
+constexpr int kMaxNb = 128;
+
+template <class F>
+__device__ __forceinline__ bool for_each_in_range_ordered(const DevArrays& a, const SceneDev& S, float4 xi,
+                                                           F&& f) {
+    unsigned long long lst[kMaxNb];
+    int cnt = 0;
+    bool overflow = false;
+    Cell c = cell_of(S, xi.x, xi.y, xi.z);
+    for_each_candidate(a, S, c, [&](uint32_t j, float4 xj) {
+        float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+        if (s <= S.smax) {
+            if (cnt < kMaxNb)
+                lst[cnt++] = ((unsigned long long)(uint32_t)__float_as_int(xj.w) << 32) | j;
+            else
+                overflow = true;
+        }
+    });
+    for (int q = 1; q < cnt; ++q) {
+        unsigned long long v = lst[q];
+        int r = q - 1;
+        while (r >= 0 && lst[r] > v) {
+            lst[r + 1] = lst[r];
+            --r;
+        }
+        lst[r + 1] = v;
+    }
+    const float4* sp = a.spos + S.p_off;
+    for (int q = 0; q < cnt; ++q) {
+        uint32_t j = (uint32_t)(lst[q] & 0xffffffffu);
+        f(j, __ldg(sp + j));
+    }
+    return !overflow;
+}
+
+// kernDefault for an in-range pair (fluid_system.h:410-416), times MASS.
+__device__ __forceinline__ float density_term(const SceneDev& S, float len) {
+    return fm(S.mass, fm(S.c_poly6, pow3(fs(S.hh, fm(len, len)))));
+}
+
+struct ForceAcc {
+    float fpx, fpy, fpz;
+    float fvx, fvy, fvz;
+    float nx, ny, nz;
+    float cfl;
+    int nb;
+    int any;
+};
+
+// Terms of passes 2 and 3 for one in-range pair (fluid_system.h:139-171):
+// r = x_i - x_j, len = |r|; vj, Aj = P_j/rho_j^2, Bj = m/rho_j.
+__device__ __forceinline__ void force_pair(const SceneDev& S, ForceAcc& acc, float rx, float ry, float rz,
+                                           float len, float vix, float viy, float viz, float Ai, float4 vj,
+                                           float Aj, float Bj, int idj, bool self) {
+    // pass 3: colour-field Laplacian, self included (laplDefault, :424-428)
+    {
+        float ld = fm(fm(-S.c_grad, fs(S.hh, fm(len, len))),
+                      fs(fm(fm(3.0f, S.h), S.h), fm(fm(7.0f, len), len)));
+        acc.cfl = fa(acc.cfl, fm(Bj, ld));
+    }
+    if (self) return;
+    acc.nb = max(acc.nb, idj);
+    acc.any = 1;
+    // gradPressure (:430-447)
+    float gx, gy, gz;
+    const float pw2 = pow2(fs(S.h, len));
+    if (len < S.cthr) {
+        float t = fm(fm(S.inv_sqrt3, S.c_spiky), pw2);
+        gx = -t;
+        gy = -t;
+        gz = -t;
+    } else {
+        float inv = fdv(1.0f, len);  // glm::normalize: r * (1 / sqrt(dot(r, r)))
+        gx = -fm(fm(fm(rx, inv), S.c_spiky), pw2);
+        gy = -fm(fm(fm(ry, inv), S.c_spiky), pw2);
+        gz = -fm(fm(fm(rz, inv), S.c_spiky), pw2);
+    }
+    const float coef = fm(fa(Ai, Aj), S.mass);
+    acc.fpx = fa(acc.fpx, fm(coef, gx));
+    acc.fpy = fa(acc.fpy, fm(coef, gy));
+    acc.fpz = fa(acc.fpz, fm(coef, gz));
+    // laplVisc (:449-453)
+    const float lv = fm(S.c_spiky, fs(S.h, len));
+    acc.fvx = fa(acc.fvx, fm(fm(fs(vj.x, vix), Bj), lv));
+    acc.fvy = fa(acc.fvy, fm(fm(fs(vj.y, viy), Bj), lv));
+    acc.fvz = fa(acc.fvz, fm(fm(fs(vj.z, viz), Bj), lv));
+    // gradDefault (:418-422)
+    const float pw = pow2(fs(S.hh, fm(len, len)));
+    acc.nx = fa(acc.nx, fm(Bj, -fm(fm(rx, S.c_grad), pw)));
+    acc.ny = fa(acc.ny, fm(Bj, -fm(fm(ry, S.c_grad), pw)));
+    acc.nz = fa(acc.nz, fm(Bj, -fm(fm(rz, S.c_grad), pw)));
+}
+
+struct TSample {
+    float y;
+    float nx, ny, nz;
+    int vnear;
+};
+
+// Heightfield surface at (x, z): bilinear over the vertex grid spanning the
+// box floor (the repository's own contact model; the reference's
+// Grid::collision is disabled at fluid_system.h:335-340).
+__device__ __forceinline__ TSample terrain_at(const SceneDev& S, const float* hs, float x, float z) {
+    TSample t;
+    float fx = fm(fs(x, S.t_xlo), S.t_isx);
+    float fz = fm(fs(z, S.t_zlo), S.t_isz);
+    if (!(fx > 0.0f)) fx = 0.0f;
+    if (fx > S.t_wmax) fx = S.t_wmax;
+    if (!(fz > 0.0f)) fz = 0.0f;
+    if (fz > S.t_dmax) fz = S.t_dmax;
+    int i0 = (int)fx, j0 = (int)fz;
+    if (i0 > S.tw - 2) i0 = S.tw - 2;
+    if (j0 > S.td - 2) j0 = S.td - 2;
+    const float tx = fs(fx, (float)i0), tz = fs(fz, (float)j0);
+    const float* r0 = hs + S.t_off + (size_t)j0 * S.tw + i0;
+    const float h00 = __ldg(r0), h10 = __ldg(r0 + 1);
+    const float h01 = __ldg(r0 + S.tw), h11 = __ldg(r0 + S.tw + 1);
+    const float a0 = fa(h00, fm(tx, fs(h10, h00)));
+    const float a1 = fa(h01, fm(tx, fs(h11, h01)));
+    const float hgt = fa(a0, fm(tz, fs(a1, a0)));
+    t.y = fa(S.t_ylo, hgt);
+    const float dx = fm(fa(fs(h10, h00), fm(tz, fs(fs(h11, h01), fs(h10, h00)))), S.t_isx);
+    const float dz = fm(fs(a1, a0), S.t_isz);
+    const float il = fdv(1.0f, fsq(fa(fa(fm(dx, dx), 1.0f), fm(dz, dz))));
+    t.nx = fm(-dx, il);
+    t.ny = il;
+    t.nz = fm(-dz, il);
+    int in = (int)fa(fx, 0.5f), jn = (int)fa(fz, 0.5f);
+    if (in > S.tw - 1) in = S.tw - 1;
+    if (jn > S.td - 1) jn = S.td - 1;
+    t.vnear = jn * S.tw + in;
+    return t;
+}
+
+// collisionS (fluid_system.h:355-407) for a box with centre c, half extents
+// l and axis weights w (exactly 1 for the reference's cube).
+__device__ __forceinline__ bool box_collide(const SceneDev& S, float px, float py, float pz, float* cp,
+                                            float* nrm) {
+    const float q[3] = {fs(px, S.box_c[0]), fs(py, S.box_c[1]), fs(pz, S.box_c[2])};
+    const float aq[3] = {fabsf(q[0]), fabsf(q[1]), fabsf(q[2])};
+    if (aq[0] < S.box_l[0] && aq[1] < S.box_l[1] && aq[2] < S.box_l[2]) return false;
+    const float m0 = fm(aq[0], S.box_w[0]), m1 = fm(aq[1], S.box_w[1]), m2 = fm(aq[2], S.box_w[2]);
+    int ax = 0;
+    float maxp = m0;
+    if (maxp < m1) {
+        ax = 1;
+        maxp = m1;
+    }
+    if (maxp < m2) ax = 2;
+    cp[0] = px;
+    cp[1] = py;
+    cp[2] = pz;
+    nrm[0] = nrm[1] = nrm[2] = 0.0f;
+    float v, s;
+    if (q[ax] < -S.box_l[ax]) {
+        v = fs(S.box_c[ax], S.box_l[ax]);
+        s = 1.0f;
+    } else {
+        v = fa(S.box_c[ax], S.box_l[ax]);
+        s = -1.0f;
+    }
+    cp[ax] = v;
+    nrm[ax] = s;
+    return true;
+}
+
+__device__ __forceinline__ float len3(float x, float y, float z) { return fsq(dist2(x, y, z)); }
+
+// ---------------------------------------------------------------------------
+// keys: cell key of each particle, its slot within the cell (warp-aggregated
+// atomics) and the per-chunk totals that the scan needs.
+__global__ void __launch_bounds__(kMaxTile) k_keys(DevArrays a) {
+    const int nwork = *a.n_ptiles;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        const int i = wk.start + threadIdx.x;
+        const bool valid = i < S.p_off + S.n;
+        const unsigned mask = __ballot_sync(kFull, valid);
+        if (!valid) continue;
+        const float4 x = a.pos[i];
+        const Cell c = cell_of(S, x.x, x.y, x.z);
+        const uint32_t k = row_key(a.tab, S, c.cy, c.cz) + (uint32_t)c.cx;
+        const uint32_t gk = (uint32_t)S.k_off + k;
+        const unsigned peers = __match_any_sync(mask, gk);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(a.counts + gk, (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        a.key[i] = k;
+        a.slot[i] = base + (uint32_t)__popc(peers & lt);
+        const uint32_t ck = (uint32_t)S.c_off + (k >> kChunkBits);
+        const unsigned cpeers = __match_any_sync(mask, ck);
+        if (lane == __ffs(cpeers) - 1) atomicAdd(a.chunk_sum + ck, (uint32_t)__popc(cpeers));
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    uint32_t t = 0;
+#pragma unroll
+    for (int q = 0; q < NT / 32; ++q) t += sh[q];
+    return t;
+}
+
+template <int NT>
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t u = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += u;
+    }
+    __syncthreads();
+    if (lane == 31) sh[wid] = inc;
+    __syncthreads();
+    uint32_t before = 0;
+#pragma unroll
+    for (int q = 0; q < NT / 32; ++q)
+        if (q < wid) before += sh[q];
+    return before + inc - v;
+}
+
+// scan: exclusive prefix of the per-key counts within each scene, one chunk
+// of kChunk keys per work item.  The chunk's offset is the sum of the earlier
+// chunk totals of its scene, so no block waits on another.  Counts are
+// cleared for the next step.
+__global__ void __launch_bounds__(kScanThreads) k_scan(DevArrays a) {
+    __shared__ uint32_t sh[kScanThreads / 32];
+    const int nwork = *a.n_ctiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ctiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        const int c = wk.start;
+        uint32_t pre = 0;
+        for (int j = threadIdx.x; j < c; j += kScanThreads) pre += a.chunk_sum[S.c_off + j];
+        pre = block_sum<kScanThreads>(pre, sh);
+        const size_t base = (size_t)S.k_off + (size_t)c * kChunk + (size_t)threadIdx.x * 16;
+        uint4* cp = reinterpret_cast<uint4*>(a.counts + base);
+        uint32_t v[16];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint4 t = cp[q];
+            v[4 * q] = t.x;
+            v[4 * q + 1] = t.y;
+            v[4 * q + 2] = t.z;
+            v[4 * q + 3] = t.w;
+        }
+        uint32_t run = 0;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            uint32_t t = v[q];
+            v[q] = run;
+            run += t;
+        }
+        const uint32_t add = pre + block_exclusive<kScanThreads>(run, sh);
+        uint4* op = reinterpret_cast<uint4*>(a.offsets + base);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            op[q] = make_uint4(v[4 * q] + add, v[4 * q + 1] + add, v[4 * q + 2] + add, v[4 * q + 3] + add);
+            cp[q] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __syncthreads();
+    }
+}
+
+// scatter: place each particle's index at its cell's offset + slot, and clear
+// the chunk totals (the scan that read them has finished).
+__global__ void __launch_bounds__(kMaxTile) k_scatter(DevArrays a) {
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        const int i = wk.start + threadIdx.x;
+        if (i < S.p_off + S.n) {
+            const uint32_t dst = a.offsets[S.k_off + a.key[i]] + a.slot[i];
+            if (dst < (uint32_t)S.n)
+                a.perm[S.p_off + dst] = (uint32_t)i;
+            else
+                atomicOr(a.status, 2u);  // inconsistent counts: never write out of range
+        }
+        const int t = (wk.start - S.p_off) / (int)blockDim.x;
+        const int ntiles = (S.n + (int)blockDim.x - 1) / (int)blockDim.x;
+        for (int j = t * (int)blockDim.x + (int)threadIdx.x; j < S.nchunks; j += ntiles * (int)blockDim.x)
+            a.chunk_sum[S.c_off + j] = 0u;
+    }
+}
+
+// reorder: make the order within each cell stable (ascending previous index,
+// so results never depend on atomic arrival order) and gather the state into
+// the sorted arrays.
+__global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        const int p = wk.start + threadIdx.x;
+        if (p >= S.p_off + S.n) continue;
+        const uint32_t i = a.perm[p];
+        if (i < (uint32_t)S.p_off || i >= (uint32_t)(S.p_off + S.n)) {
+            atomicOr(a.status, 2u);
+            continue;
+        }
+        const uint32_t k = a.key[i];
+        const uint32_t st = a.offsets[S.k_off + k];
+        const uint32_t en = min(a.offsets[S.k_off + k + 1], (uint32_t)S.n);
+        const uint32_t* cell = a.perm + S.p_off;
+        uint32_t r = 0;
+        for (uint32_t q = st; q < en; ++q) r += (cell[q] < i) ? 1u : 0u;
+        if (st + r >= (uint32_t)S.n) {
+            atomicOr(a.status, 2u);
+            continue;
+        }
+        const int dst = S.p_off + (int)(st + r);
+        a.spos[dst] = a.pos[i];
+        a.svel[dst] = a.vel[i];
+        if (S.flags & kFlagRecord) a.snbid[dst] = a.nbid[i];
+    }
+}
+
+// density: pass 1 (fluid_system.h:107-124), then the per-particle factors the
+// force pass reuses: P/rho^2 and m/rho.
+template <bool ORDERED>
+__global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
+        const int p = wk.start + threadIdx.x;
+        if (p >= S.p_off + S.n) continue;
+        const float4 xi = a.spos[p];
+        float rho = 0.0f;
+        auto term = [&](uint32_t, float4 xj) {
+            float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+            if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
+        };
+        if (ORDERED) {
+            if (!for_each_in_range_ordered(a, S, xi, term)) atomicOr(a.status, 1u);
+        } else {
+            for_each_candidate(a, S, cell_of(S, xi.x, xi.y, xi.z), term);
+        }
+        const float P = fm(S.k, fs(rho, S.p0));
+        a.dyn[p] = make_float4(rho, fdv(P, fm(rho, rho)), fdv(S.mass, rho), P);
+    }
+}
+
+// force: passes 2 and 3 (fluid_system.h:127-178) and advance (:306-353) with
+// the terrain contact, the box collision and the erosion exchange.
+template <bool ORDERED>
+__global__ void __launch_bounds__(kMaxTile) k_force(DevArrays a) {
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
+        const int p = wk.start + threadIdx.x;
+        if (p >= S.p_off + S.n) continue;
+        const int pl = p - S.p_off;
+        const float4 xi = a.spos[p];
+        const float4 vi = a.svel[p];
+        const float4 di = a.dyn[p];
+        const float rho = di.x, Ai = di.y;
+        ForceAcc acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, -1, 0};
+        const float4* sv = a.svel + S.p_off;
+        const float4* sd = a.dyn + S.p_off;
+        auto term = [&](uint32_t j, float4 xj) {
+            const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
+            const float s = dist2(rx, ry, rz);
+            if (s <= S.smax) {
+                const float4 vj = __ldg(sv + j);
+                const float4 dj = __ldg(sd + j);
+                force_pair(S, acc, rx, ry, rz, fsq(s), vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z,
+                           __float_as_int(xj.w), (int)j == pl);
+            }
+        };
+        if (ORDERED) {
+            if (!for_each_in_range_ordered(a, S, xi, term)) atomicOr(a.status, 1u);
+        } else {
+            for_each_candidate(a, S, cell_of(S, xi.x, xi.y, xi.z), term);
+        }
+        // pass-2 results (:151-154) and pass 3 (:163, :177)
+        const float Fpx = -fm(acc.fpx, rho), Fpy = -fm(acc.fpy, rho), Fpz = -fm(acc.fpz, rho);
+        const float Fvx = fm(acc.fvx, S.visc), Fvy = fm(acc.fvy, S.visc), Fvz = fm(acc.fvz, S.visc);
+        const float Fgx = fm(rho, S.g[0]), Fgy = fm(rho, S.g[1]), Fgz = fm(rho, S.g[2]);
+        const float nsig = fm(-S.sigma, acc.cfl);
+        const float Fsx = fm(nsig, acc.nx), Fsy = fm(nsig, acc.ny), Fsz = fm(nsig, acc.nz);
+        // advance (:318-331)
+        const float Fx = fa(fa(Fpx, Fvx), fa(Fgx, Fsx));
+        const float Fy = fa(fa(Fpy, Fvy), fa(Fgy, Fsy));
+        const float Fz = fa(fa(Fpz, Fvz), fa(Fgz, Fsz));
+        const float ax = fdv(Fx, rho), ay = fdv(Fy, rho), az = fdv(Fz, rho);
+        const float dt = S.dt;
+        float vx = fa(vi.x, fm(ax, dt)), vy = fa(vi.y, fm(ay, dt)), vz = fa(vi.z, fm(az, dt));
+        float px = fa(xi.x, fm(vx, dt)), py = fa(xi.y, fm(vy, dt)), pz = fa(xi.z, fm(vz, dt));
+
+        const bool has_t = (S.flags & kFlagTerrain) != 0;
+        TSample ts;
+        if (has_t) {
+            ts = terrain_at(S, a.theight, px, pz);
+            if (py < ts.y && dt != 0.0f) {
+                const float d = fs(ts.y, py);
+                const float vdn = fa(fa(fm(vx, ts.nx), fm(vy, ts.ny)), fm(vz, ts.nz));
+                if (vdn < 0.0f) {
+                    const float sp = len3(vx, vy, vz);
+                    const float f = fa(1.0f, sp > 0.0f ? fdv(fm(S.cr, d), fm(dt, sp)) : 0.0f);
+                    vx = fs(vx, fm(fm(ts.nx, f), vdn));
+                    vy = fs(vy, fm(fm(ts.ny, f), vdn));
+                    vz = fs(vz, fm(fm(ts.nz, f), vdn));
+                }
+                py = ts.y;
+            }
+        }
+        {
+            float cp[3], nr[3];
+            if (box_collide(S, px, py, pz, cp, nr) && dt != 0.0f) {
+                const float d = len3(fs(px, cp[0]), fs(py, cp[1]), fs(pz, cp[2]));
+                const float f = fa(1.0f, fdv(fm(0.5f, d), fm(dt, len3(vx, vy, vz))));
+                const float vdn = fa(fa(fm(vx, nr[0]), fm(vy, nr[1])), fm(vz, nr[2]));
+                vx = fs(vx, fm(fm(nr[0], f), vdn));
+                vy = fs(vy, fm(fm(nr[1], f), vdn));
+                vz = fs(vz, fm(fm(nr[2], f), vdn));
+                px = cp[0];
+                py = cp[1];
+                pz = cp[2];
+            }
+        }
+        int sed = __float_as_int(vi.w);
+        if (has_t && (S.flags & kFlagErosion)) {
+            const float e = fs(py, ts.y);
+            if (e <= S.layer) {
+                float capf = fm(S.k_capacity, len3(vx, vy, vz));
+                if (capf > 1.0f) capf = 1.0f;
+                const float cap = fm(capf, 1073741824.0f);
+                const float s = __int2float_rn(sed);
+                const float q = (s < cap) ? fm(fm(S.k_pick, dt), fs(cap, s)) : -fm(fm(S.k_dep, dt), fs(s, cap));
+                if (q == q) {
+                    long long Q = __float2ll_rn(q);
+                    if ((long long)sed + Q < 0) Q = -(long long)sed;
+                    if ((long long)sed + Q > 1073741824LL) Q = 1073741824LL - (long long)sed;
+                    if (Q != 0) {
+                        sed += (int)Q;
+                        atomicAdd(reinterpret_cast<unsigned long long*>(a.tdelta + S.t_off + ts.vnear),
+                                  (unsigned long long)(-Q));
+                    }
+                }
+            }
+        }
+        a.pos[p] = make_float4(px, py, pz, xi.w);
+        a.vel[p] = make_float4(vx, vy, vz, __int_as_float(sed));
+        if (S.flags & kFlagRecord) {
+            float* r = a.rec + (size_t)p * kRecFloats;
+            r[0] = ax; r[1] = ay; r[2] = az;
+            r[3] = Fpx; r[4] = Fpy; r[5] = Fpz;
+            r[6] = Fvx; r[7] = Fvy; r[8] = Fvz;
+            r[9] = Fgx; r[10] = Fgy; r[11] = Fgz;
+            r[12] = Fsx; r[13] = Fsy; r[14] = Fsz;
+            r[15] = acc.nx; r[16] = acc.ny; r[17] = acc.nz;
+            a.nbid[p] = acc.any ? acc.nb : a.snbid[p];
+        }
+    }
+}
+
+// terrain: height snapshot = base + delta * unit, read by the next step.
+__global__ void __launch_bounds__(kMaxTile) k_terrain(DevArrays a) {
+    const int nwork = *a.n_ttiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ttiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        const int t = wk.start + threadIdx.x;
+        if (t >= S.t_off + S.tw * S.td) continue;
+        a.theight[t] = fa(a.tbase[t], fm(__ll2float_rn(a.tdelta[t]), S.height_unit));
+    }
+}
+
+__global__ void k_tick(int* steps_left, int nscenes) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nscenes && steps_left[s] > 0) steps_left[s] -= 1;
+}
+
+__global__ void __launch_bounds__(kMaxTile) k_neighbour_counts(DevArrays a, int32_t* out) {
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        const SceneDev& S = a.scenes[wk.scene];
+        const int p = wk.start + threadIdx.x;
+        if (p >= S.p_off + S.n) continue;
+        const float4 xi = a.spos[p];
+        const int pl = p - S.p_off;
+        int cnt = 0;
+        for_each_candidate(a, S, cell_of(S, xi.x, xi.y, xi.z), [&](uint32_t j, float4 xj) {
+            float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+            if (s <= S.smax && (int)j != pl) ++cnt;
+        });
+        const int id = __float_as_int(xi.w);
+        if (id >= 0 && id < S.n) out[S.p_off + id] = cnt;
+    }
+}
+
+// FP64 diagnostics: kDiagBlocks blocks per listed scene write fixed-order
+// partial sums (so the result is reproducible); integer totals use int64
+// atomics, which are exact in any order.
+__global__ void __launch_bounds__(256) k_diag(DevArrays a, double* partial, long long* isums, int* nan_count) {
+    __shared__ double sh[kDiagDoubles][8];
+    const int li = blockIdx.x / kDiagBlocks, b = blockIdx.x % kDiagBlocks;
+    const int sidx = a.scene_list[li];
+    const SceneDev& S = a.scenes[sidx];
+    double acc[kDiagDoubles] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long sed = 0, ter = 0;
+    int nan = 0;
+    const double m = (double)S.mass;
+    for (int q = b * 256 + threadIdx.x; q < S.n; q += kDiagBlocks * 256) {
+        const float4 x = a.pos[S.p_off + q];
+        const float4 v = a.vel[S.p_off + q];
+        const double vx = v.x, vy = v.y, vz = v.z;
+        acc[0] += m * vx;
+        acc[1] += m * vy;
+        acc[2] += m * vz;
+        acc[3] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        acc[4] += -m * ((double)S.g[0] * x.x + (double)S.g[1] * x.y + (double)S.g[2] * x.z);
+        sed += (long long)__float_as_int(v.w);
+        if (!isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z)) ++nan;
+    }
+    if (S.flags & kFlagTerrain)
+        for (int t = b * 256 + threadIdx.x; t < S.tw * S.td; t += kDiagBlocks * 256) ter += a.tdelta[S.t_off + t];
+    for (int c = 0; c < kDiagDoubles; ++c) {
+        double v = acc[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+        if ((threadIdx.x & 31) == 0) sh[c][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kDiagDoubles) {
+        double v = 0.0;
+        for (int q = 0; q < 8; ++q) v += sh[threadIdx.x][q];
+        partial[(size_t)blockIdx.x * kDiagDoubles + threadIdx.x] = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sed += __shfl_down_sync(kFull, sed, o);
+        ter += __shfl_down_sync(kFull, ter, o);
+        nan += __shfl_down_sync(kFull, nan, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (sed) atomicAdd(reinterpret_cast<unsigned long long*>(isums + 2 * li), (unsigned long long)sed);
+        if (ter) atomicAdd(reinterpret_cast<unsigned long long*>(isums + 2 * li + 1), (unsigned long long)ter);
+        if (nan) atomicAdd(nan_count + li, nan);
+    }
+}
+
+}  // namespace
+
+void launch_keys(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_keys<<<s.grid_p, s.tile, 0, st>>>(a);
+}
+void launch_scan(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_scan<<<s.grid_c, kScanThreads, 0, st>>>(a);
+}
+void launch_scatter(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_scatter<<<s.grid_p, s.tile, 0, st>>>(a);
+}
+void launch_reorder(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_reorder<<<s.grid_p, s.tile, 0, st>>>(a);
+}
+void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_density<false><<<s.grid_p, s.tile, 0, st>>>(a);
+}
+void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_density<true><<<s.grid_p, s.tile, 0, st>>>(a);
+}
+void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_force<false><<<s.grid_p, s.tile, 0, st>>>(a);
+}
+void launch_force_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_force<true><<<s.grid_p, s.tile, 0, st>>>(a);
+}
+void launch_terrain(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    k_terrain<<<s.grid_t, s.tile, 0, st>>>(a);
+}
+void launch_tick(const DevArrays& a, int nscenes, cudaStream_t st) {
+    k_tick<<<(nscenes + 127) / 128, 128, 0, st>>>(a.steps_left, nscenes);
+}
+void launch_neighbour_counts(const DevArrays& a, const LaunchShape& s, int32_t* out_by_id, cudaStream_t st) {
+    k_neighbour_counts<<<s.grid_p, s.tile, 0, st>>>(a, out_by_id);
+}
+void launch_diag(const DevArrays& a, int nlist, double* partial, long long* isums, int* nan_count,
+                 cudaStream_t st) {
+    if (nlist > 0) k_diag<<<nlist * kDiagBlocks, 256, 0, st>>>(a, partial, isums, nan_count);
+}
+
+}  // namespace sph

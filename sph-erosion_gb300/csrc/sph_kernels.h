@@ -1,0 +1,72 @@
+// Kernel launchers of the simulation step (implemented in sph_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sph_types.h"
+
+namespace sph {
+
+// Device pointers of one system's arenas, passed by value to every launcher.
+struct DevArrays {
+    const SceneDev* scenes;
+    int* steps_left;          // per scene: -1 unlimited, 0 inactive, >0 remaining
+    const Work* ptiles;       // particle tiles
+    const int* n_ptiles;
+    const Work* ctiles;       // scan chunks (start = chunk index within the scene)
+    const int* n_ctiles;
+    const Work* ttiles;       // terrain tiles
+    const int* n_ttiles;
+    const int* scene_list;    // active scene ids (diagnostics)
+    // particles
+    float4* pos;   // x y z id(bits)      current state
+    float4* vel;   // vx vy vz sediment(bits)
+    float4* spos;  // sorted copies
+    float4* svel;
+    float4* dyn;   // density, P/rho^2, m/rho, P
+    uint32_t* key;
+    uint32_t* slot;
+    uint32_t* perm;
+    int32_t* nbid;
+    int32_t* snbid;
+    float* rec;    // kRecFloats per particle (record mode)
+    // keys
+    uint32_t* counts;
+    uint32_t* offsets;
+    uint32_t* chunk_sum;
+    const uint32_t* tab;
+    // terrain
+    const float* tbase;
+    long long* tdelta;
+    float* theight;
+    // status word: bit 0 = ordered-mode neighbour overflow
+    unsigned* status;
+};
+
+struct LaunchShape {
+    int tile;        // threads per particle tile
+    int grid_p;      // persistent grid of particle kernels
+    int grid_c;      // persistent grid of the scan
+    int grid_t;      // persistent grid of the terrain kernel
+};
+
+void launch_keys(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_scan(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_scatter(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_reorder(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_force_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_terrain(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
+void launch_tick(const DevArrays& a, int nscenes, cudaStream_t st);
+
+// Inspection and on-demand kernels.
+void launch_neighbour_counts(const DevArrays& a, const LaunchShape& s, int32_t* out_by_id, cudaStream_t st);
+// Per-scene FP64 partial sums: kDiagBlocks blocks per listed scene.
+constexpr int kDiagBlocks = 32;
+constexpr int kDiagDoubles = 8;  // mass-weighted momentum xyz, kinetic, potential, (pad)
+void launch_diag(const DevArrays& a, int nlist, double* partial, long long* isums, int* nan_count,
+                 cudaStream_t st);
+
+}  // namespace sph

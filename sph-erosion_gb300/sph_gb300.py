@@ -1,0 +1,325 @@
+"""ctypes binding of libsph_gb300.so (include/sph_erosion.h).
+
+The product path is the CUDA library; this module only marshals arguments.
+Loading fails loudly when the library has not been built: there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsph_gb300.so")
+
+SPH_FLAG_RECORD = 1
+SPH_FLAG_ORDERED = 2
+ERRORS = {-1: "invalid", -2: "cuda", -3: "nomem", -4: "capacity", -5: "state", -6: "device"}
+
+
+class SphError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sph error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("gravity", C.c_float * 3), ("dt", C.c_float), ("rest_density", C.c_float), ("mass", C.c_float),
+        ("viscosity", C.c_float), ("surface_tension", C.c_float), ("gas_stiffness", C.c_float),
+        ("restitution", C.c_float), ("smoothing_radius", C.c_float), ("box_center", C.c_float * 3),
+        ("box_half", C.c_float * 3), ("cell_mult", C.c_float), ("erosion", C.c_int), ("k_capacity", C.c_float),
+        ("k_pickup", C.c_float), ("k_deposit", C.c_float), ("erosion_layer", C.c_float), ("flags", C.c_int),
+    ]
+
+
+class Particle(C.Structure):
+    _fields_ = [
+        ("id", C.c_int), ("position", C.c_float * 3), ("velocity", C.c_float * 3),
+        ("acceleration", C.c_float * 3), ("density", C.c_float), ("pressure", C.c_float),
+        ("pressure_force", C.c_float * 3), ("viscosity_force", C.c_float * 3), ("gravity_force", C.c_float * 3),
+        ("surface_force", C.c_float * 3), ("surface_normal", C.c_float * 3), ("neighb_id", C.c_int),
+        ("sediment", C.c_int32),
+    ]
+
+
+class Diag(C.Structure):
+    _fields_ = [
+        ("fluid_mass", C.c_double), ("momentum", C.c_double * 3), ("kinetic", C.c_double),
+        ("potential", C.c_double), ("sediment_units", C.c_int64), ("terrain_units", C.c_int64),
+        ("total_units", C.c_int64), ("unit_volume", C.c_double), ("n", C.c_int32), ("nan_particles", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {"fluid_mass": self.fluid_mass, "momentum": tuple(self.momentum), "kinetic": self.kinetic,
+                "potential": self.potential, "sediment_units": self.sediment_units,
+                "terrain_units": self.terrain_units, "total_units": self.total_units,
+                "unit_volume": self.unit_volume, "n": self.n, "nan_particles": self.nan_particles}
+
+
+class SystemConfig(C.Structure):
+    _fields_ = [
+        ("device", C.c_int), ("particle_capacity", C.c_int64), ("key_capacity", C.c_int64),
+        ("terrain_capacity", C.c_int64), ("max_scenes", C.c_int), ("tile", C.c_int), ("graph_steps", C.c_int),
+        ("hbm_budget", C.c_int64),
+    ]
+
+
+_lib = None
+SIGNATURES = {
+    "sph_last_error": (C.c_char_p, []),
+    "sph_params_default": (None, [C.POINTER(Params)]),
+    "sph_system_config_default": (None, [C.POINTER(SystemConfig)]),
+    "sph_system_create": (C.c_int, [C.POINTER(SystemConfig), C.POINTER(C.c_void_p)]),
+    "sph_system_destroy": (C.c_int, [C.c_void_p]),
+    "sph_system_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "sph_system_sync": (C.c_int, [C.c_void_p]),
+    "sph_system_time_steps": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
+    "sph_system_profile_stages": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "sph_system_memory": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sph_scene_create": (C.c_int, [C.c_void_p, C.POINTER(Params), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "sph_scene_destroy": (C.c_int, [C.c_void_p, C.c_int]),
+    "sph_scene_set_params": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Params)]),
+    "sph_scene_get_params": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Params)]),
+    "sph_scene_set_steps": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "sph_scene_get_steps": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "sph_scene_set_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "sph_scene_add_lattice": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]),
+    "sph_scene_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "sph_scene_get_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sph_scene_get_particle": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(Particle)]),
+    "sph_scene_get_records": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "sph_scene_diag": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Diag)]),
+    "sph_scene_set_terrain": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "sph_scene_gen_terrain": (C.c_int, [C.c_void_p, C.c_int, C.c_uint64, C.c_int, C.c_float, C.c_float, C.c_float,
+                                        C.c_int]),
+    "sph_scene_get_terrain": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "sph_scene_terrain_dims": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sph_scene_debug_sort": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "sph_scene_neighbour_counts": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "sph_scene_grid_dims": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+}
+
+
+def lib():
+    """Load libsph_gb300.so; raise if it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is not built; run build() first")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ck(rc: int):
+    if rc != 0:
+        raise SphError(rc, lib().sph_last_error().decode())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def default_params(**overrides) -> Params:
+    """Reference defaults (fluid_system.h:460-479) with keyword overrides;
+    vector fields take 3-sequences."""
+    p = Params()
+    lib().sph_params_default(C.byref(p))
+    for k, v in overrides.items():
+        if k in ("gravity", "box_center", "box_half"):
+            getattr(p, k)[:] = [float(x) for x in v]
+        elif k == "box_len":
+            p.box_half[:] = [float(v)] * 3
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def params_dict(p: Params) -> dict:
+    d = {}
+    for name, _ in Params._fields_:
+        v = getattr(p, name)
+        d[name] = tuple(v) if not isinstance(v, (int, float)) else v
+    return d
+
+
+class System:
+    def __init__(self, particle_capacity=1 << 16, key_capacity=1 << 16, terrain_capacity=1 << 12, max_scenes=1024,
+                 tile=256, graph_steps=16, hbm_budget=0, device=0):
+        cfg = SystemConfig()
+        lib().sph_system_config_default(C.byref(cfg))
+        cfg.device, cfg.particle_capacity, cfg.key_capacity = device, particle_capacity, key_capacity
+        cfg.terrain_capacity, cfg.max_scenes, cfg.tile = terrain_capacity, max_scenes, tile
+        cfg.graph_steps, cfg.hbm_budget = graph_steps, hbm_budget
+        h = C.c_void_p()
+        _ck(lib().sph_system_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().sph_system_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def scene(self, params: Params, capacity=0, terrain=(0, 0)) -> "Scene":
+        sid = C.c_int()
+        _ck(lib().sph_scene_create(self.h, C.byref(params), int(capacity), int(terrain[0]), int(terrain[1]),
+                                   C.byref(sid)))
+        return Scene(self, sid.value)
+
+    def step(self, n=1):
+        _ck(lib().sph_system_step(self.h, int(n)))
+
+    def sync(self):
+        _ck(lib().sph_system_sync(self.h))
+
+    def time_steps(self, n) -> float:
+        ms = C.c_float()
+        _ck(lib().sph_system_time_steps(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    def profile_stages(self, n) -> np.ndarray:
+        out = np.zeros(8, np.float32)
+        _ck(lib().sph_system_profile_stages(self.h, int(n), _p(out)))
+        return out
+
+    def memory(self) -> int:
+        b = C.c_int64()
+        _ck(lib().sph_system_memory(self.h, C.byref(b)))
+        return b.value
+
+
+STAGES = ["keys", "scan", "scatter", "reorder", "density", "force", "terrain", "tick"]
+
+
+class Scene:
+    def __init__(self, system: System, sid: int):
+        self.sys = system
+        self.id = sid
+
+    @property
+    def h(self):
+        return self.sys.h
+
+    def destroy(self):
+        _ck(lib().sph_scene_destroy(self.h, self.id))
+
+    def set_params(self, p: Params):
+        _ck(lib().sph_scene_set_params(self.h, self.id, C.byref(p)))
+
+    def params(self) -> Params:
+        p = Params()
+        _ck(lib().sph_scene_get_params(self.h, self.id, C.byref(p)))
+        return p
+
+    def set_steps(self, n):
+        _ck(lib().sph_scene_set_steps(self.h, self.id, int(n)))
+
+    def steps(self) -> int:
+        v = C.c_int()
+        _ck(lib().sph_scene_get_steps(self.h, self.id, C.byref(v)))
+        return v.value
+
+    def set_particles(self, pos, vel=None):
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        _ck(lib().sph_scene_set_particles(self.h, self.id, len(pos), _p(pos), _p(v)))
+
+    def add_lattice(self, n, origin=(0.0, 0.0, 0.0)) -> int:
+        o = np.asarray(origin, np.float32)
+        added = C.c_int()
+        _ck(lib().sph_scene_add_lattice(self.h, self.id, int(n), _p(o), C.byref(added)))
+        return added.value
+
+    def count(self) -> int:
+        v = C.c_int()
+        _ck(lib().sph_scene_count(self.h, self.id, C.byref(v)))
+        return v.value
+
+    def get_particles(self):
+        n = self.count()
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        dens = np.zeros(n, np.float32)
+        sed = np.zeros(n, np.int32)
+        _ck(lib().sph_scene_get_particles(self.h, self.id, _p(pos), _p(vel), _p(dens), _p(sed)))
+        return dict(pos=pos, vel=vel, density=dens, sed=sed)
+
+    def get_positions(self, out=None):
+        n = self.count()
+        out = np.zeros((n, 3), np.float32) if out is None else out
+        _ck(lib().sph_scene_get_particles(self.h, self.id, _p(out), None, None, None))
+        return out
+
+    def get_records(self):
+        n = self.count()
+        rec = np.zeros((n, 27), np.float32)
+        nb = np.zeros(n, np.int32)
+        _ck(lib().sph_scene_get_records(self.h, self.id, _p(rec), _p(nb)))
+        return rec, nb
+
+    def get_particle(self, pid) -> Particle:
+        out = Particle()
+        _ck(lib().sph_scene_get_particle(self.h, self.id, int(pid), C.byref(out)))
+        return out
+
+    def diag(self) -> dict:
+        d = Diag()
+        _ck(lib().sph_scene_diag(self.h, self.id, C.byref(d)))
+        return d.as_dict()
+
+    def set_terrain(self, heights):
+        hgt = np.ascontiguousarray(heights, np.float32)
+        d, w = hgt.shape
+        _ck(lib().sph_scene_set_terrain(self.h, self.id, int(w), int(d), _p(hgt)))
+
+    def gen_terrain(self, seed, octaves, amplitude, lacunarity=2.0, gain=0.5, kind=0):
+        _ck(lib().sph_scene_gen_terrain(self.h, self.id, int(seed), int(octaves), float(amplitude),
+                                        float(lacunarity), float(gain), int(kind)))
+
+    def terrain_dims(self):
+        w, d = C.c_int(), C.c_int()
+        _ck(lib().sph_scene_terrain_dims(self.h, self.id, C.byref(w), C.byref(d)))
+        return w.value, d.value
+
+    def get_terrain(self):
+        w, d = self.terrain_dims()
+        hgt = np.zeros((d, w), np.float32)
+        dl = np.zeros((d, w), np.int64)
+        _ck(lib().sph_scene_get_terrain(self.h, self.id, _p(hgt), _p(dl)))
+        return hgt, dl
+
+    def debug_sort(self):
+        n = self.count()
+        keys = np.zeros(n, np.uint32)
+        order = np.zeros(n, np.int32)
+        _ck(lib().sph_scene_debug_sort(self.h, self.id, _p(keys), _p(order)))
+        return keys, order
+
+    def neighbour_counts(self):
+        out = np.zeros(self.count(), np.int32)
+        _ck(lib().sph_scene_neighbour_counts(self.h, self.id, _p(out)))
+        return out
+
+    def grid_dims(self):
+        out = np.zeros(4, np.int32)
+        _ck(lib().sph_scene_grid_dims(self.h, self.id, _p(out)))
+        return tuple(int(x) for x in out)

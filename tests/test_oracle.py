@@ -1,0 +1,225 @@
+"""CPU tests: the oracle is pinned against the reference's golden vectors and
+the known answers derived from the reference's code."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+REF = dict(g=(0.0, -9.82, 0.0), dt=0.01, p0=998.29, mass=0.02, visc=3.5, surf_tens=0.0728, k=3.0, cr=0.5,
+           h=0.0457)
+C1 = dict(g=(0.0, -9.81, 0.0), dt=1e-3, p0=1000.0, mass=float(np.float32(1000.0 * 0.02 ** 3)), visc=0.1,
+          surf_tens=0.0728, k=3.0, cr=0.5, h=0.04)
+
+
+def ref_params(O, **kw):
+    d = dict(REF)
+    d.update(kw)
+    ln = d.pop("len", 0.2)
+    return O.make_params(box_l=(ln, ln, ln), **d)
+
+
+def test_oracle_default_scene_bit_exact(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_default_1000.npz")
+    p = ref_params(O)
+    out = O.run(p, g["pos0"], nsteps=1)
+    assert np.array_equal(out["rec"], g["rec1"])
+    assert np.array_equal(out["nbid"], g["nb1"])
+    out = O.run(p, g["pos0"], nsteps=10)
+    assert np.array_equal(out["rec"], g["rec10"])
+    assert np.array_equal(out["nbid"], g["nb10"])
+
+
+def test_oracle_default_scene_50_steps(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_default_1000.npz")
+    out = O.run(ref_params(O), g["pos0"], nsteps=50)
+    assert np.array_equal(out["pos"], g["pos50"][:, 0:3])
+    assert np.array_equal(out["vel"], g["pos50"][:, 3:6])
+    assert np.array_equal(out["nbid"], g["nb50"])
+
+
+def test_oracle_plain_2048_bit_exact(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_c1_2048.npz")
+    p = O.make_params(box_l=(0.5, 0.5, 0.5), **C1)
+    out = O.run(p, g["pos0"], nsteps=1)
+    assert np.array_equal(out["rec"], g["rec1"])
+    out = O.run(p, g["pos0"], nsteps=100)
+    assert np.array_equal(out["rec"], g["rec100"])
+    assert np.array_equal(out["nbid"], g["nb100"])
+
+
+def test_oracle_plain_16384_one_step(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_c1_16384.npz")
+    p = O.make_params(box_l=(0.5, 0.5, 0.5), **C1)
+    out = O.run(p, g["pos0"], nsteps=1)
+    assert np.array_equal(out["rec"], g["rec1"])
+    assert np.array_equal(out["nbid"], g["nb1"])
+
+
+def test_oracle_edge_cases_bit_exact(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_edge.npz")
+    p = ref_params(O)
+    out = O.run(p, g["coinc0"], nsteps=1)
+    assert np.array_equal(out["rec"], g["coinc_rec1"])
+    assert np.array_equal(out["nbid"], g["coinc_nb1"])
+    out = O.run(p, g["coinc0"], nsteps=5)
+    assert np.array_equal(out["rec"], g["coinc_rec5"])
+    out = O.run(p, g["lone0"], nsteps=3)
+    assert np.array_equal(out["rec"], g["lone_rec3"])
+    out = O.run(p, g["walls0"], g["walls_vel0"], nsteps=1)
+    assert np.array_equal(out["rec"], g["walls_rec1"])
+
+
+def test_neighbour_counts_match_reference(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_c1_2048.npz")
+    cnt = O.neighbour_counts(g["rec100"][:, 0:3], 0.04)
+    assert np.array_equal(cnt, g["cnt100"])
+
+
+# ---- known answers derived from the reference's code -----------------------
+
+def test_poly6_normalisation_fp64():
+    """kernDefault (fluid_system.h:415) integrates to 1 over the ball of radius h."""
+    h = 0.0457
+    c = 315.0 / (64.0 * math.pi * h ** 9)
+    r = np.linspace(0.0, h, 200001)
+    f = c * (h * h - r * r) ** 3 * 4.0 * math.pi * r * r
+    integral = np.trapezoid(f, r)
+    assert abs(integral - 1.0) < 1e-6
+
+
+def test_lattice_density_closed_form(oracle_lib):
+    """A particle inside a cubic lattice at spacing h/2 has exactly 32
+    neighbours (i^2+j^2+k^2 <= 4), and its density is the closed-form poly6
+    sum over those offsets.  The spacing is a power of two so that lattice
+    distances (and the distance h itself) are exact in FP32."""
+    O = oracle_lib
+    s = 1.0 / 64.0
+    h = 2 * s
+    pos = (np.stack(np.meshgrid(*[np.arange(7)] * 3, indexing="ij"), -1).reshape(-1, 3) * s).astype(np.float32)
+    centre = int(np.argmin(np.abs(pos - pos.mean(0)).sum(1)))
+    cnt = O.neighbour_counts(pos, h)
+    assert cnt[centre] == 32
+    p = O.make_params(h=h, mass=0.004, p0=1000.0, box_l=(1.0, 1.0, 1.0))
+    out = O.run(p, pos, nsteps=1, precision="f64")
+    pi = float(np.float32(3.141592))
+    cpoly = 315.0 / (64.0 * pi * float(np.float32(h)) ** 9)
+    offs = [(i, j, k) for i in range(-2, 3) for j in range(-2, 3) for k in range(-2, 3) if i * i + j * j + k * k <= 4]
+    hh = float(np.float32(h)) ** 2
+    expect = sum(float(np.float32(0.004)) * cpoly * (hh - float(np.float32(s)) ** 2 * (i * i + j * j + k * k)) ** 3 for i, j, k in offs)
+    assert abs(out["rec"][centre, 9] - expect) / expect < 1e-5
+
+
+def test_free_fall(oracle_lib):
+    """One isolated particle: a = g exactly, v = g dt, x = x0 + g dt^2."""
+    O = oracle_lib
+    p = ref_params(O)
+    out = O.run(p, np.array([[0.0, 0.1, 0.0]], np.float32), nsteps=1)
+    assert np.array_equal(out["rec"][0, 6:9], np.array([0.0, -9.82, 0.0], np.float32))
+    assert out["vel"][0, 1] == np.float32(np.float32(-9.82) * np.float32(0.01))
+
+
+def test_box_reflection(oracle_lib):
+    """A particle crossing x = len is clamped and reflected by the law at
+    fluid_system.h:345 (gravity off so that the velocity stays on the x axis)."""
+    O = oracle_lib
+    p = ref_params(O, g=(0.0, 0.0, 0.0))
+    out = O.run(p, np.array([[0.195, 0.0, 0.0]], np.float32), np.array([[1.0, 0.0, 0.0]], np.float32), nsteps=1)
+    assert out["pos"][0, 0] == np.float32(0.2)
+    v = np.float32(1.0)
+    xn = np.float32(np.float32(0.195) + v * np.float32(0.01))
+    d = np.float32(xn - np.float32(0.2))
+    f = np.float32(1) + np.float32(np.float32(0.5) * d) / np.float32(np.float32(0.01) * v)
+    assert out["vel"][0, 0] == np.float32(v - f * v)
+
+
+def test_coincident_direction(oracle_lib):
+    """Coincident particles push along normalize(1,1,1) (fluid_system.h:438-440)."""
+    O = oracle_lib
+    p = ref_params(O)
+    pos = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 0.0]], np.float32)
+    out = O.run(p, pos, nsteps=1)
+    fp = out["rec"][:, 11:14]
+    assert np.all(fp[0] == fp[0][0]) and fp[0][0] != 0
+
+
+# ---- grid restatement ---------------------------------------------------------
+
+def test_keys_and_stable_order(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_c1_16384.npz")
+    p = O.make_params(box_l=(0.5, 0.5, 0.5), **C1)
+    grd = O.grid(p, 1.0)
+    pos = g["state100"][:, 0:3]
+    keys = O.cell_keys(grd, pos)
+    assert keys.max() < grd.nkeys - 1
+    perm = O.stable_sort(keys, grd.nkeys)
+    assert np.array_equal(perm, np.argsort(keys, kind="stable"))
+    # every neighbour pair lies within one cell on each axis
+    cell = np.floor((pos - np.array(grd.lo)) * np.float32(grd.inv_cell)).astype(np.int64)
+    i, j = np.nonzero(np.linalg.norm(pos[:200, None, :] - pos[None, :, :], axis=2) <= 0.04)
+    assert np.abs(cell[i] - cell[j]).max() <= 1
+
+
+def test_fbm_deterministic_and_bounded(oracle_lib):
+    O = oracle_lib
+    a = O.fbm(0, 128, 128, 4, 0.2)
+    b = O.fbm(0, 128, 128, 4, 0.2)
+    c = O.fbm(1, 128, 128, 4, 0.2)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert a.min() >= 0.0 and a.max() < 0.2
+    r = O.fbm(3, 64, 64, 6, 0.5, kind=1)
+    assert r.min() >= 0.0 and r.max() <= 0.5
+
+
+def test_mesh_matches_reference(oracle_lib, golden):
+    O = oracle_lib
+    g = golden("ref_mesh.npz")
+    dx, dy, dz = (int(v) for v in g["dims"])
+    verts, idx = O.mesh(g["hmap"], dx, dy, dz)
+    assert np.array_equal(verts, g["surface"])
+    assert np.array_equal(idx, g["indices"])
+
+
+def test_erosion_conserves_mass_exactly(oracle_lib):
+    """Sediment plus terrain units are conserved exactly by the oracle."""
+    O = oracle_lib
+    import workloads as W
+
+    n = 600
+    pos = W.scaled_block(n, box_half=(0.25, 0.25, 0.25), amp=0.05)
+    tw = td = 24
+    base = O.fbm(5, tw, td, 3, 0.05).ravel()
+    prm = O.make_params(box_l=(0.25, 0.25, 0.25), terrain=(tw, td), height_unit=1e-6, erosion=True,
+                        k_capacity=0.05, k_pickup=5.0, k_deposit=2.0, layer=0.04, **C1)
+    vel = np.zeros_like(pos)
+    vel[:, 0] = 1.5
+    out = O.run(prm, pos, vel, nsteps=40, base=base)
+    assert out["sed"].sum() > 0
+    assert int(out["sed"].astype(np.int64).sum()) + int(out["delta"].sum()) == 0
+
+
+def test_reference_harness_matches_when_present(oracle_lib):
+    """Where the reference sources exist, the harness and the oracle agree on
+    a fresh seeded case too (not only on the committed vectors)."""
+    O = oracle_lib
+    if not os.path.isdir("/root/reference"):
+        pytest.skip("reference sources absent")
+    O.build_ref()
+    rng = np.random.default_rng(11)
+    pos = rng.uniform(-0.15, 0.15, (300, 3)).astype(np.float32)
+    R = O.Reference()
+    R.set_params(**REF)
+    R.set_particles(pos)
+    R.run(3)
+    rec, _, nb = R.get()
+    out = O.run(ref_params(O), pos, nsteps=3)
+    assert np.array_equal(out["rec"], rec) and np.array_equal(out["nbid"], nb)
