@@ -194,6 +194,9 @@ def run_ours(args, spec, config):
             tot += sysm.time_steps(1)
         tot_s = barrier_max(tot / 1e3, ws)
     value = ws * n * args.steps / tot_s
+    if args.kernels_only:
+        sysm.sync()
+        return
     # per-stage device times of the same steps (events on the launching stream)
     stages = sysm.profile_stages(max(3, min(args.steps, 10)))
     # e2e: through the C ABI with host buffers, copies inside the timed region
@@ -254,6 +257,8 @@ def main():
     ap.add_argument("--workload", default="plain_1m", choices=["plain_1m", "plain_small"])
     ap.add_argument("--tile", type=int, default=256)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="warm-up and timed steps only (for profiler captures); prints nothing")
     args = ap.parse_args()
     import workloads as W
 
