@@ -177,6 +177,7 @@ def run_ours(args, spec, config):
     n = spec["n"]
     sysm = S.System(particle_capacity=n, key_capacity=1 << 20, terrain_capacity=1 << 21, tile=args.tile,
                     graph_steps=16, device=local)
+    spec = dict(spec, params=dict(spec["params"], cell_mult=args.cell_mult))
     sc = W.build_scene(sysm, spec)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     # warm-up
@@ -255,7 +256,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain_1m", choices=["plain_1m", "plain_small"])
-    ap.add_argument("--tile", type=int, default=256)
+    ap.add_argument("--tile", type=int, default=512)
+    ap.add_argument("--cell-mult", type=float, default=0.5)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--kernels-only", action="store_true",
                     help="warm-up and timed steps only (for profiler captures); prints nothing")

@@ -169,6 +169,8 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
     SPH_CK(cudaSetDevice(dev_));
     SPH_CK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
     SPH_CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    configure_kernels();
+    SPH_CK(cudaGetLastError());
     pa_.reset(0);
     ka_.reset(0);
     ca_.reset(0);
@@ -366,6 +368,14 @@ void System::fill_dev(Scene& sc) {
     if (p.flags & SPH_FLAG_ORDERED) d.flags |= kFlagOrdered;
     for (int a = 0; a < 3; ++a) d.lo[a] = sc.lo[a];
     d.inv_cell = sc.inv_cell;
+    // h in cell units for the row trimming, enlarged by 1e-5 relative plus four
+    // ulps of the largest in-grid cell coordinate, so that the FP32 rounding of
+    // the two particles' cell coordinates can never drop a neighbour
+    {
+        const float tmax = (float)std::max(sc.nx, std::max(sc.ny, sc.nz));
+        const double ulp = (double)std::nextafter(tmax, INFINITY) - (double)tmax;
+        d.hcell = (float)((double)p.smoothing_radius * (double)sc.inv_cell * (1.0 + 1e-5) + 4.0 * ulp + 1e-4);
+    }
     // kernel constants, same FP32 expressions as fluid_system.h:415-452
     // with PI = 3.141592f (Erosion/sphere.h:8)
     const float h = p.smoothing_radius;
@@ -430,7 +440,7 @@ static void validate(const sph_params& p) {
     for (int a = 0; a < 3; ++a)
         if (!(p.box_half[a] > 0.0f) || !std::isfinite(p.box_half[a]))
             throw Error(SPH_ERR_INVALID, "box_half must be positive");
-    if (!(p.cell_mult >= 0.5f) || !(p.cell_mult <= 8.0f)) throw Error(SPH_ERR_INVALID, "cell_mult must be in [0.5, 8]");
+    if (!(p.cell_mult >= 0.25f) || !(p.cell_mult <= 8.0f)) throw Error(SPH_ERR_INVALID, "cell_mult must be in [0.25, 8]");
 }
 
 int System::create_scene(const sph_params& p, int capacity, int tw, int td) {

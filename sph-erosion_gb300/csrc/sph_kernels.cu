@@ -76,27 +76,126 @@ __device__ __forceinline__ uint32_t row_key(const uint32_t* tab, const SceneDev&
     return (__ldg(tab + S.tab_off + cy) | __ldg(tab + S.tab_off + S.ny + cz)) * (uint32_t)S.nx;
 }
 
-// Visit every particle in the (2R+1)^3 cells around c, cell rows merged
-// along x (x-adjacent cells of a row are contiguous in key order).  f(j, xj)
-// receives the scene-local sorted index and the position.
+// A particle's position in cell units before flooring and clamping, and its
+// cell.
+struct Probe {
+    Cell c;
+    float tx, ty, tz;
+    bool finite;
+};
+
+__device__ __forceinline__ Probe probe_of(const SceneDev& S, float4 x) {
+    Probe q;
+    q.tx = fm(fs(x.x, S.lo[0]), S.inv_cell);
+    q.ty = fm(fs(x.y, S.lo[1]), S.inv_cell);
+    q.tz = fm(fs(x.z, S.lo[2]), S.inv_cell);
+    q.finite = (q.tx == q.tx) && (q.ty == q.ty) && (q.tz == q.tz);
+    q.c = cell_of(S, x.x, x.y, x.z);
+    return q;
+}
+
+// Distance in cell units from coordinate t to cell k of an axis of n cells.
+// The two end cells reach to infinity: positions outside the grid are
+// clamped into them.
+__device__ __forceinline__ float cell_gap(float t, int k, int n) {
+    float g = 0.0f;
+    if (k > 0 && t < (float)k) g = (float)k - t;
+    if (k < n - 1 && t > (float)(k + 1)) g = t - (float)(k + 1);
+    return g;
+}
+
+// Cells [xl, xh] of row (y, z) that the h-sphere around the particle can
+// reach; false when it reaches none.  Conservative (h enlarged by hcell's
+// slack), so only out-of-range candidates are ever dropped and the in-range
+// visiting order is the same as for the full (2R+1)^3 block.
+__device__ __forceinline__ bool row_span(const SceneDev& S, const Probe& q, int y, int z, int* xl, int* xh) {
+    if (!q.finite) return false;  // a NaN position has no neighbour, itself included
+    const float gy = cell_gap(q.ty, y, S.ny), gz = cell_gap(q.tz, z, S.nz);
+    const float r2 = S.hcell * S.hcell - gy * gy - gz * gz;
+    if (!(r2 >= 0.0f)) return false;
+    const float r = sqrtf(r2);
+    const float top = (float)(S.nx - 1);
+    const float lo = fminf(fmaxf(floorf(q.tx - r), 0.0f), top);
+    const float hi = fminf(fmaxf(floorf(q.tx + r), 0.0f), top);
+    *xl = (int)lo;
+    *xh = (int)hi;
+    return true;
+}
+
+// Visit every candidate of the (2R+1)^2 cell rows around the particle,
+// trimmed to the h-sphere (x-adjacent cells of a row are contiguous in key
+// order).  f(j, xj) receives the scene-local sorted index and the position.
 template <class F>
-__device__ __forceinline__ void for_each_candidate(const DevArrays& a, const SceneDev& S, Cell c, F&& f) {
+__device__ __forceinline__ void for_each_candidate(const DevArrays& a, const SceneDev& S, const Probe& q, F&& f) {
     const int R = S.reach;
     const uint32_t* off = a.offsets + S.k_off;
     const float4* sp = a.spos + S.p_off;
-    const int xl = max(c.cx - R, 0), xh = min(c.cx + R, S.nx - 1);
     for (int dz = -R; dz <= R; ++dz) {
-        const int z = c.cz + dz;
+        const int z = q.c.cz + dz;
         if (z < 0 || z >= S.nz) continue;
         for (int dy = -R; dy <= R; ++dy) {
-            const int y = c.cy + dy;
+            const int y = q.c.cy + dy;
             if (y < 0 || y >= S.ny) continue;
+            int xl, xh;
+            if (!row_span(S, q, y, z, &xl, &xh)) continue;
             const uint32_t row = row_key(a.tab, S, y, z);
             const uint32_t st = __ldg(off + row + xl);
             const uint32_t en = __ldg(off + row + xh + 1);
             for (uint32_t j = st; j < en; ++j) f(j, __ldg(sp + j));
         }
     }
+}
+
+// In-range traversal of the fast path.  Candidates are tested in a tight
+// loop and the indices of in-range ones are compacted into a per-thread list
+// in shared memory (column threadIdx.x, so lanes touch distinct banks); the
+// costly pair terms then run over the list with every lane of the warp busy
+// instead of diverging on each candidate.  The visiting order is the
+// candidate order, so the sums are the same as a direct traversal.
+//
+// All lanes of a warp visit the same (dz, dy) cell row at the same time and
+// step through it for the longest lane's length, so the list drain is a
+// collective step: it runs as soon as any lane's list is full, with all lanes
+// draining theirs.  Every lane of the warp must call this function (lanes
+// without a particle pass valid = false).
+constexpr int kListCap = 32;
+
+template <class F>
+__device__ __forceinline__ void for_each_in_range_listed(const DevArrays& a, const SceneDev& S, bool valid,
+                                                         float4 xi, uint32_t* list, F&& f) {
+    const int R = S.reach;
+    const Probe pr = probe_of(S, xi);
+    const uint32_t* off = a.offsets + S.k_off;
+    const float4* sp = a.spos + S.p_off;
+    uint32_t* my = list + threadIdx.x;
+    const int stride = blockDim.x;
+    int cnt = 0;
+    for (int dz = -R; dz <= R; ++dz) {
+        for (int dy = -R; dy <= R; ++dy) {
+            const int z = pr.c.cz + dz, y = pr.c.cy + dy;
+            uint32_t st = 0, len = 0;
+            int xl, xh;
+            if (valid && z >= 0 && z < S.nz && y >= 0 && y < S.ny && row_span(S, pr, y, z, &xl, &xh)) {
+                const uint32_t row = row_key(a.tab, S, y, z);
+                st = __ldg(off + row + xl);
+                len = __ldg(off + row + xh + 1) - st;
+            }
+            const uint32_t maxlen = __reduce_max_sync(kFull, len);
+            for (uint32_t t = 0; t < maxlen; ++t) {
+                if (t < len) {
+                    const uint32_t j = st + t;
+                    const float4 xj = __ldg(sp + j);
+                    const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+                    if (s <= S.smax) my[(cnt++) * stride] = j;
+                }
+                if (__any_sync(kFull, cnt == kListCap)) {
+                    for (int q = 0; q < cnt; ++q) f(my[q * stride]);
+                    cnt = 0;
+                }
+            }
+        }
+    }
+    for (int q = 0; q < cnt; ++q) f(my[q * stride]);
 }
 
 // Ordered (validation) traversal: collect in-range candidates, sort them by
@@ -110,7 +209,7 @@ __device__ __forceinline__ bool for_each_in_range_ordered(const DevArrays& a, co
     unsigned long long lst[kMaxNb];
     int cnt = 0;
     bool overflow = false;
-    Cell c = cell_of(S, xi.x, xi.y, xi.z);
+    const Probe c = probe_of(S, xi);
     for_each_candidate(a, S, c, [&](uint32_t j, float4 xj) {
         float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
         if (s <= S.smax) {
@@ -436,6 +535,7 @@ __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
 // force pass reuses: P/rho^2 and m/rho.
 template <bool ORDERED>
 __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
+    extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = a.ptiles[w];
@@ -443,17 +543,23 @@ __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
         const SceneDev& S = a.scenes[wk.scene];
         if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
         const int p = wk.start + threadIdx.x;
-        if (p >= S.p_off + S.n) continue;
-        const float4 xi = a.spos[p];
+        const bool valid = p < S.p_off + S.n;
+        if (ORDERED && !valid) continue;
+        const float4 xi = a.spos[valid ? p : S.p_off];
         float rho = 0.0f;
-        auto term = [&](uint32_t, float4 xj) {
-            float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
-            if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
-        };
         if (ORDERED) {
+            auto term = [&](uint32_t, float4 xj) {
+                float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+                if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
+            };
             if (!for_each_in_range_ordered(a, S, xi, term)) atomicOr(a.status, 1u);
         } else {
-            for_each_candidate(a, S, cell_of(S, xi.x, xi.y, xi.z), term);
+            // the density term is cheap: a direct traversal beats compaction
+            if (!valid) continue;
+            for_each_candidate(a, S, probe_of(S, xi), [&](uint32_t, float4 xj) {
+                const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+                if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
+            });
         }
         const float P = fm(S.k, fs(rho, S.p0));
         a.dyn[p] = make_float4(rho, fdv(P, fm(rho, rho)), fdv(S.mass, rho), P);
@@ -464,36 +570,40 @@ __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
 // the terrain contact, the box collision and the erosion exchange.
 template <bool ORDERED>
 __global__ void __launch_bounds__(kMaxTile) k_force(DevArrays a) {
+    extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = a.ptiles[w];
         if (a.steps_left[wk.scene] == 0) continue;
         const SceneDev& S = a.scenes[wk.scene];
         if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
-        const int p = wk.start + threadIdx.x;
-        if (p >= S.p_off + S.n) continue;
+        const int p0 = wk.start + threadIdx.x;
+        const bool valid = p0 < S.p_off + S.n;
+        if (ORDERED && !valid) continue;
+        const int p = valid ? p0 : S.p_off;
         const int pl = p - S.p_off;
         const float4 xi = a.spos[p];
         const float4 vi = a.svel[p];
         const float4 di = a.dyn[p];
         const float rho = di.x, Ai = di.y;
         ForceAcc acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, -1, 0};
+        const float4* sp = a.spos + S.p_off;
         const float4* sv = a.svel + S.p_off;
         const float4* sd = a.dyn + S.p_off;
-        auto term = [&](uint32_t j, float4 xj) {
+        auto pair = [&](uint32_t j, float4 xj) {
             const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
             const float s = dist2(rx, ry, rz);
-            if (s <= S.smax) {
-                const float4 vj = __ldg(sv + j);
-                const float4 dj = __ldg(sd + j);
-                force_pair(S, acc, rx, ry, rz, fsq(s), vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z,
-                           __float_as_int(xj.w), (int)j == pl);
-            }
+            const float4 vj = __ldg(sv + j);
+            const float4 dj = __ldg(sd + j);
+            force_pair(S, acc, rx, ry, rz, fsq(s), vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z, __float_as_int(xj.w),
+                       (int)j == pl);
         };
         if (ORDERED) {
-            if (!for_each_in_range_ordered(a, S, xi, term)) atomicOr(a.status, 1u);
+            // the ordered list holds only in-range candidates
+            if (!for_each_in_range_ordered(a, S, xi, pair)) atomicOr(a.status, 1u);
         } else {
-            for_each_candidate(a, S, cell_of(S, xi.x, xi.y, xi.z), term);
+            for_each_in_range_listed(a, S, valid, xi, list, [&](uint32_t j) { pair(j, __ldg(sp + j)); });
+            if (!valid) continue;
         }
         // pass-2 results (:151-154) and pass 3 (:163, :177)
         const float Fpx = -fm(acc.fpx, rho), Fpy = -fm(acc.fpy, rho), Fpz = -fm(acc.fpz, rho);
@@ -605,7 +715,7 @@ __global__ void __launch_bounds__(kMaxTile) k_neighbour_counts(DevArrays a, int3
         const float4 xi = a.spos[p];
         const int pl = p - S.p_off;
         int cnt = 0;
-        for_each_candidate(a, S, cell_of(S, xi.x, xi.y, xi.z), [&](uint32_t j, float4 xj) {
+        for_each_candidate(a, S, probe_of(S, xi), [&](uint32_t j, float4 xj) {
             float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
             if (s <= S.smax && (int)j != pl) ++cnt;
         });
@@ -677,6 +787,14 @@ void launch_scatter(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
 void launch_reorder(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     k_reorder<<<s.grid_p, s.tile, 0, st>>>(a);
 }
+void configure_kernels() {
+    const int bytes = kListCap * kMaxTile * (int)sizeof(uint32_t);
+    cudaFuncSetAttribute(k_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.tile * sizeof(uint32_t); }
+
 void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     k_density<false><<<s.grid_p, s.tile, 0, st>>>(a);
 }
@@ -684,7 +802,7 @@ void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream
     k_density<true><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_force<false><<<s.grid_p, s.tile, 0, st>>>(a);
+    k_force<false><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
 }
 void launch_force_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     k_force<true><<<s.grid_p, s.tile, 0, st>>>(a);

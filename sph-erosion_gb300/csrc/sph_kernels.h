@@ -50,6 +50,9 @@ struct LaunchShape {
     int grid_t;      // persistent grid of the terrain kernel
 };
 
+// Once per process and device: opt the list-traversal kernels into >48 KB of
+// dynamic shared memory.
+void configure_kernels();
 void launch_keys(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
 void launch_scan(const DevArrays& a, const LaunchShape& s, cudaStream_t st);
 void launch_scatter(const DevArrays& a, const LaunchShape& s, cudaStream_t st);

@@ -39,6 +39,7 @@ struct SceneDev {
     // grid
     float lo[3];
     float inv_cell;
+    float hcell;             // h in cell units, enlarged to cover FP32 rounding (row trimming)
     // physics (Erosion/fluid_system.h:460-479)
     float h, hh;             // h and h*h
     float smax;              // largest s with sqrtf(s) <= h: s <= smax <=> length <= h
