@@ -185,6 +185,33 @@ SPH_API int sph_scene_neighbour_counts(sph_system* s, int scene, int32_t* counts
 /* Grid dims used by the sort: nx ny nz nkeys. */
 SPH_API int sph_scene_grid_dims(sph_system* s, int scene, int* dims4);
 
+/* ---- allocation-free density pass ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory themselves or let a library do it: a host application that owns the
+ * whole GPU through its own memory pool, a real-time loop that cannot take
+ * cudaMalloc's implicit device synchronisation, or a plugin running where
+ * allocation is not allowed.  Computes the reference's pass 1 (density and
+ * pressure of every particle, fluid_system.h:107-124; no motion) for n
+ * particles given as 3n floats in DEVICE memory, writing n densities (and,
+ * if pressure_dev is not NULL, n pressures) to DEVICE memory in input order.
+ * It runs the same sort and density kernels as a scene step, on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream), and returns after the
+ * stream has drained.  It allocates nothing: its scratch is one fixed device
+ * array of SPH_STATIC_SCRATCH_BYTES that every GPU loading the library holds
+ * until the process exits.  Limits: n <= SPH_STATIC_MAX_PARTICLES and a
+ * uniform grid of at most SPH_STATIC_MAX_KEYS keys; larger requests return
+ * SPH_ERR_CAPACITY.  The first call on a device resolves the array's device
+ * address with that device current; make that first call before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * (other streams or host threads) race and must be serialised by the
+ * caller. */
+#define SPH_STATIC_MAX_PARTICLES 32768
+#define SPH_STATIC_MAX_KEYS 262144
+#define SPH_STATIC_MAX_TABLE 4096
+#define SPH_STATIC_SCRATCH_BYTES 5131008
+SPH_API int sph_density_static(const sph_params* p, int n, const float* pos3_dev, float* density_dev,
+                               float* pressure_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

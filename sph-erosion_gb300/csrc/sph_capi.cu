@@ -281,3 +281,8 @@ int sph_scene_grid_dims(sph_system* s, int scene, int* dims4) {
 }
 
 }  // extern "C"
+
+namespace sph {
+// Lets other translation units report through sph_last_error().
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace sph

@@ -104,11 +104,14 @@ class System {
     unsigned read_status();
     void check_status();
 
+    // Uniform grid and device descriptor of a scene; they depend on the
+    // scene's parameters and ranges only.
+    static void geometry(Scene& sc);
+    static void fill_dev(Scene& sc);
+
    private:
     Scene& scene(int id);
     const Scene& scene(int id) const;
-    void geometry(Scene& sc);
-    void fill_dev(Scene& sc);
     void upload_scene(int id);
     void ensure_particle_cap(Scene& sc, int need);
     void ensure_arena(RangeAlloc& ra, int64_t need, int which);
@@ -171,6 +174,9 @@ class System {
 // Host implementation of the seeded fBm generator (sph_terrain.cpp).
 void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, float lacunarity, float gain,
                  int kind, float* out);
+
+// Sets the calling thread's sph_last_error() message (sph_capi.cu).
+void set_last_error(const std::string& msg);
 
 // Host FP32 constants of a scene (sph_engine.cu): exposed for inspection.
 float smax_for(float h);

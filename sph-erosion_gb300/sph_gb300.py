@@ -100,6 +100,7 @@ SIGNATURES = {
     "sph_scene_debug_sort": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "sph_scene_neighbour_counts": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "sph_scene_grid_dims": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "sph_density_static": (C.c_int, [C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 
