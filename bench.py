@@ -249,22 +249,95 @@ def run_ours(args, spec, config):
 C_PARAMS_BYTES = 4 * 24
 
 
+def run_batched(args, config):
+    """Batched form vs plain form on the same seeded scenes: all scenes in one
+    system (one launch per stage for all of them, 16-step CUDA graphs) against
+    each scene alone in its own system, timed scene after scene."""
+    import torch
+
+    import sph_gb300 as S
+    import workloads as W
+
+    torch.cuda.set_device(0)
+    reqs = W.batched_requests(args.scenes)
+    total = sum(r["particles"] for r in reqs)
+    base = W.base_params(args.cell_mult)
+    sysm = S.System(particle_capacity=total + 512 * len(reqs), key_capacity=1 << 24, terrain_capacity=1 << 24,
+                    tile=args.tile, graph_steps=16)
+    for r in reqs:
+        sysm.scene_from_request(base, r)
+    sysm.step(args.warmup)
+    sysm.sync()
+    with Clocks() as clk:
+        ms = sysm.time_steps(args.steps)
+    batched = total * args.steps / (ms * 1e-3)
+    sysm.close()
+    # plain form: one system per scene, same steps
+    plain_ms = 0.0
+    for r in reqs:
+        with S.System(particle_capacity=r["particles"], tile=args.tile, graph_steps=16) as one:
+            one.scene_from_request(base, r)
+            one.step(args.warmup)
+            one.sync()
+            plain_ms += one.time_steps(args.steps)
+    plain = total * args.steps / (plain_ms * 1e-3)
+    line = {"metric": METRIC, "value": batched, "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
+            "config": dict(config, workload="batched", scenes=len(reqs), particles=total,
+                           l2="inputs larger than L2 (%.0f MB of particle state)" % (total * 100 / 1e6)),
+            "plain_value": plain, "batched_over_plain": batched / plain, "plain_ms_per_step": plain_ms / args.steps,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args, config):
+    """Served form: a Poisson request trace replayed in real time through the
+    continuous-batching server."""
+    import sph_gb300 as S
+    import workloads as W
+
+    trace = W.serving_trace(args.requests, rate=args.rate)
+    with Clocks() as clk, S.Server(W.base_params(args.cell_mult), tile=args.tile, chunk_steps=16,
+                                    hbm_budget=120 << 30) as srv:
+        res, st = srv.run_trace(trace)
+    bad = sum(1 for r in res if r.total_units != 0 or r.nan_particles != 0)
+    line = {"metric": METRIC, "value": st["throughput"], "unit": "particle-steps/s", "n_gpus": 1,
+            "steps": int(sum(r["steps"] for r in trace)), "warmup": 0, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Poisson request trace)",
+            "config": dict(config, workload="serving", requests=len(trace), rate_per_s=args.rate,
+                           hbm_budget_gb=120),
+            "p50_latency_s": st["p50_s"], "p99_latency_s": st["p99_s"], "max_latency_s": st["max_s"],
+            "wall_s": st["wall_s"], "peak_active": st["peak_active"], "peak_particles": st["peak_particles"],
+            "peak_bytes": st["peak_bytes"], "chunks": st["chunks"], "mass_violations": bad,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plain_1m", choices=["plain_1m", "plain_small"])
+    ap.add_argument("--workload", default="plain_1m", choices=["plain_1m", "plain_small", "batched", "serving"])
     ap.add_argument("--tile", type=int, default=512)
     ap.add_argument("--cell-mult", type=float, default=0.5)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
+    ap.add_argument("--requests", type=int, default=400, help="serving: requests in the trace")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
     ap.add_argument("--kernels-only", action="store_true",
                     help="warm-up and timed steps only (for profiler captures); prints nothing")
     args = ap.parse_args()
     import workloads as W
 
-    spec = W.plain_1m() if args.workload == "plain_1m" else W.plain_small()
+    if args.workload in ("batched", "serving") and args.impl == "ours":
+        cfg = {"h": W.H, "dt": W.PHYS["dt"], "erosion": True, "tile": args.tile, "cell_mult": args.cell_mult}
+        (run_batched if args.workload == "batched" else run_serving)(args, cfg)
+        return
+    spec = W.plain_1m() if args.workload != "plain_small" else W.plain_small()
     t = spec.get("terrain")
     config = {"workload": spec["name"], "particles": spec["n"],
               "terrain": f"{t['w']}x{t['d']} fBm {t['octaves']} oct amp {t['amplitude']}" if t else None,

@@ -185,6 +185,80 @@ SPH_API int sph_scene_neighbour_counts(sph_system* s, int scene, int32_t* counts
 /* Grid dims used by the sort: nx ny nz nkeys. */
 SPH_API int sph_scene_grid_dims(sph_system* s, int scene, int* dims4);
 
+/* ---- seeded scenes, batching and the request server -----------------------
+ * No counterpart in the reference (a single interactive scene).  A request
+ * describes one erosion scene: a dam-break block of `particles` lattice
+ * particles at spacing h/2 placed from `seed` in a cube box, over a
+ * `terrain_side`^2 fBm heightmap (6 octaves) seeded with `seed`, run for
+ * `steps` steps. */
+typedef struct sph_request {
+    uint64_t seed;
+    int32_t particles;
+    int32_t terrain_side;
+    int32_t steps;
+    float coverage;  /* block volume / box volume above the terrain; 0 = from the seed, in [0.2, 0.5) */
+    float amplitude; /* terrain amplitude / box side; 0 = from the seed, in [0.1, 0.4) */
+    double arrival_s; /* arrival time in a replayed trace, seconds from the start */
+} sph_request;
+
+/* Create the scene a request describes in a system.  `base` gives the
+ * physical constants (h, mass, ...); its box is replaced by the recipe's. */
+SPH_API int sph_scene_from_request(sph_system* s, const sph_params* base, const sph_request* r, int* scene);
+
+typedef struct sph_server sph_server;
+
+typedef struct sph_server_config {
+    int device;
+    int tile;                     /* particles per work tile (0 = 512) */
+    float cell_mult;              /* grid cell edge / h (0 = 0.5) */
+    int chunk_steps;              /* steps per batched launch sequence (CUDA graph), 0 = 16 */
+    int64_t hbm_budget;           /* bytes the server may hold (0 = 120 GiB) */
+    int64_t max_active_particles; /* admission cap on resident particles (0 = none) */
+    int max_scenes;               /* 0 = 4096 */
+    sph_params base;              /* physical constants of every scene */
+} sph_server_config;
+
+typedef struct sph_result {
+    int64_t ticket;
+    uint64_t seed;
+    int32_t particles;
+    int32_t steps;
+    double arrival_s, admit_s, done_s; /* seconds from the server's start */
+    int64_t total_units;               /* sediment + terrain change: 0 when mass is conserved */
+    int64_t sediment_units;
+    int32_t nan_particles;
+    int32_t pad;
+    double kinetic;
+    uint64_t state_hash;               /* FNV-1a of final positions, velocities, sediment in id order */
+} sph_result;
+
+typedef struct sph_server_stats {
+    int64_t completed;
+    double wall_s;           /* first arrival to last completion */
+    double particle_steps;   /* sum of particles x steps completed */
+    double throughput;       /* particle_steps / wall_s */
+    double p50_s, p99_s, max_s; /* request latency: completion - arrival */
+    int64_t peak_bytes;      /* largest device memory held */
+    int32_t peak_active;     /* most scenes resident at once */
+    int32_t chunks;          /* batched launch sequences run */
+    int64_t peak_particles;  /* most particles resident at once */
+} sph_server_stats;
+
+SPH_API void sph_server_config_default(sph_server_config* c);
+SPH_API int sph_server_create(const sph_server_config* cfg, sph_server** out);
+SPH_API int sph_server_destroy(sph_server* s);
+/* Queue a request (its arrival_s is ignored: it arrives now). */
+SPH_API int sph_server_submit(sph_server* s, const sph_request* r, int64_t* ticket);
+/* Admit what fits, run one chunk of batched steps, retire finished scenes
+ * and copy up to `cap` completed results out; *n_out = number copied,
+ * *active = scenes still resident or queued. */
+SPH_API int sph_server_poll(sph_server* s, sph_result* out, int cap, int* n_out, int* active);
+/* Replay a trace in real time: request i arrives reqs[i].arrival_s seconds
+ * after the call starts.  Returns when every request has completed; results
+ * are in request order. */
+SPH_API int sph_server_run_trace(sph_server* s, const sph_request* reqs, int n, sph_result* results,
+                                 sph_server_stats* stats);
+
 /* ---- allocation-free density pass ----------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory themselves or let a library do it: a host application that owns the

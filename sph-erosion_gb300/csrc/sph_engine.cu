@@ -302,13 +302,27 @@ void System::ensure_arena(RangeAlloc& ra, int64_t need, int which) {
         ra.release(off, need);
         return;
     }
-    const int64_t cap = std::max(ra.cap() * 2, ra.cap() + need);
-    switch (which) {
-        case 0: grow_particles(round_up(cap, kPAlign)); break;
-        case 1: grow_keys(round_up(cap, kChunk)); break;
-        case 2: grow_chunks(cap); break;
-        case 3: grow_tables(cap); break;
-        default: grow_terrain(round_up(cap, kTAlign)); break;
+    // Double the arena; under an HBM budget fall back to growing by exactly
+    // what is missing when doubling would not fit.
+    auto grow = [&](int64_t cap) {
+        switch (which) {
+            case 0: grow_particles(round_up(cap, kPAlign)); break;
+            case 1: grow_keys(round_up(cap, kChunk)); break;
+            case 2: grow_chunks(cap); break;
+            case 3: grow_tables(cap); break;
+            default: grow_terrain(round_up(cap, kTAlign)); break;
+        }
+    };
+    const int64_t doubled = std::max(ra.cap() * 2, ra.cap() + need);
+    if (cfg_.hbm_budget > 0) {
+        try {
+            grow(doubled);
+        } catch (const Error& e) {
+            if (e.code != SPH_ERR_CAPACITY) throw;
+            grow(ra.cap() + need);
+        }
+    } else {
+        grow(doubled);
     }
 }
 

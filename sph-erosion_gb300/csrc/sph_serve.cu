@@ -1,0 +1,388 @@
+// Request server: continuous batching of erosion scenes on one GPU.
+//
+// Requests are admitted against an HBM budget (and an optional cap on
+// resident particles) at the boundary of each chunk of batched steps.  Each
+// admitted request becomes a scene of one System with its own step budget,
+// so scenes that arrive while others are on the GPU join the next chunk's
+// launches, run alongside the others and retire independently.  A scene's
+// results never depend on what it shares the GPU with: each scene's work is
+// a separate set of tiles with its own neighbour ranges.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/sph_erosion.h"
+#include "sph_engine.h"
+#include "sph_recipe.h"
+
+namespace sph {
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) {
+        h ^= b[i];
+        h *= 0x100000001B3ULL;
+    }
+    return h;
+}
+
+}  // namespace
+
+// Builds the scene of a request in `sys`; returns its id.
+int scene_from_request(System& sys, const sph_params& base, const sph_request& r) {
+    RecipeGeometry g;
+    recipe_geometry(r, base.smoothing_radius, &g);
+    sph_params p;
+    recipe_params(base, g, &p);
+    std::vector<float> pos((size_t)r.particles * 3);
+    recipe_particles(r, g, pos.data());
+    std::vector<float> hgt((size_t)r.terrain_side * r.terrain_side);
+    fbm_heights(r.seed, r.terrain_side, r.terrain_side, 6, g.amplitude, 2.0f, 0.5f, 0, hgt.data());
+    const int id = sys.create_scene(p, r.particles, r.terrain_side, r.terrain_side);
+    try {
+        sys.set_terrain(id, r.terrain_side, r.terrain_side, hgt.data());
+        sys.set_particles(id, r.particles, pos.data(), nullptr);
+    } catch (...) {
+        sys.destroy_scene(id);
+        throw;
+    }
+    return id;
+}
+
+class Server {
+   public:
+    explicit Server(const sph_server_config& c) : cfg_(c), sys_(sys_config(c)), t0_(Clock::now()) {
+        if (cfg_.chunk_steps <= 0) cfg_.chunk_steps = 16;
+        if (cfg_.hbm_budget <= 0) cfg_.hbm_budget = (int64_t)120 << 30;
+        if (cfg_.cell_mult <= 0.0f) cfg_.cell_mult = 0.5f;
+        cfg_.base.cell_mult = cfg_.cell_mult;
+    }
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0_).count(); }
+    void restart_clock() { t0_ = Clock::now(); }
+
+    int64_t submit(const sph_request& r, double arrival) {
+        if (r.particles <= 0 || r.steps < 0) throw Error(SPH_ERR_INVALID, "request needs particles > 0 and steps >= 0");
+        RecipeGeometry g;
+        recipe_geometry(r, cfg_.base.smoothing_radius, &g);  // validates early
+        Pending q{next_ticket_++, r, arrival};
+        queue_.push_back(q);
+        return q.ticket;
+    }
+
+    // One admission + chunk + retirement round.  Returns the number of
+    // requests still queued or resident.
+    int poll() {
+        admit();
+        if (!active_.empty()) {
+            sys_.step(cfg_.chunk_steps);
+            sys_.sync();
+            ++chunks_;
+            retire();
+        }
+        return (int)(queue_.size() + active_.size());
+    }
+
+    bool idle_until_arrival(double* next) const {
+        if (!active_.empty() || queue_.empty()) return false;
+        *next = queue_.front().arrival;
+        return true;
+    }
+
+    std::vector<sph_result>& done() { return done_; }
+    const sph_server_stats& stats() const { return stats_; }
+    sph_server_stats& stats() { return stats_; }
+
+   private:
+    struct Pending {
+        int64_t ticket;
+        sph_request req;
+        double arrival;
+    };
+    struct Active {
+        Pending p;
+        int scene;
+        double admit;
+        int64_t bytes;
+    };
+
+    static sph_system_config sys_config(const sph_server_config& c) {
+        sph_system_config s;
+        sph_system_config_default(&s);
+        s.device = c.device;
+        s.tile = c.tile > 0 ? c.tile : 512;
+        s.graph_steps = c.chunk_steps > 0 ? c.chunk_steps : 16;
+        s.hbm_budget = c.hbm_budget > 0 ? c.hbm_budget : ((int64_t)120 << 30);
+        s.max_scenes = c.max_scenes > 0 ? c.max_scenes : 4096;
+        // arenas start small and grow within the budget as requests arrive
+        s.particle_capacity = 1 << 16;
+        s.key_capacity = 1 << 18;
+        s.terrain_capacity = 1 << 16;
+        return s;
+    }
+
+    int64_t request_bytes(const sph_request& r) {
+        RecipeGeometry g;
+        recipe_geometry(r, cfg_.base.smoothing_radius, &g);
+        sph_params p;
+        recipe_params(cfg_.base, g, &p);
+        return sys_.scene_bytes(r.particles, r.terrain_side, r.terrain_side, p);
+    }
+
+    void admit() {
+        const double t = now();
+        while (!queue_.empty() && queue_.front().arrival <= t) {
+            const Pending& q = queue_.front();
+            const int64_t need = request_bytes(q.req);
+            if (need > cfg_.hbm_budget) throw Error(SPH_ERR_CAPACITY, "a request exceeds the whole HBM budget");
+            if (reserved_ + need > cfg_.hbm_budget) break;
+            if (cfg_.max_active_particles > 0 && !active_.empty() &&
+                resident_particles_ + q.req.particles > cfg_.max_active_particles)
+                break;
+            int id;
+            try {
+                id = scene_from_request(sys_, cfg_.base, q.req);
+            } catch (const Error& e) {
+                if (e.code == SPH_ERR_CAPACITY || e.code == SPH_ERR_NOMEM) {
+                    if (active_.empty()) throw;
+                    break;  // wait for retirements to free arena space
+                }
+                throw;
+            }
+            sys_.set_steps(id, q.req.steps);
+            active_.push_back(Active{q, id, now(), need});
+            reserved_ += need;
+            resident_particles_ += q.req.particles;
+            queue_.pop_front();
+            stats_.peak_active = std::max<int32_t>(stats_.peak_active, (int32_t)active_.size());
+            stats_.peak_particles = std::max<int64_t>(stats_.peak_particles, resident_particles_);
+            stats_.peak_bytes = std::max<int64_t>(stats_.peak_bytes, sys_.memory_bytes());
+            if (q.req.steps == 0) break;  // retire it on the next round
+        }
+    }
+
+    void retire() {
+        const double t = now();
+        std::vector<Active> keep;
+        for (Active& a : active_) {
+            if (sys_.steps(a.scene) > 0) {
+                keep.push_back(a);
+                continue;
+            }
+            sph_result r;
+            std::memset(&r, 0, sizeof r);
+            r.ticket = a.p.ticket;
+            r.seed = a.p.req.seed;
+            r.particles = a.p.req.particles;
+            r.steps = a.p.req.steps;
+            r.arrival_s = a.p.arrival;
+            r.admit_s = a.admit;
+            r.done_s = t;
+            sph_diag d;
+            sys_.diag(a.scene, &d);
+            r.total_units = d.total_units;
+            r.sediment_units = d.sediment_units;
+            r.nan_particles = d.nan_particles;
+            r.kinetic = d.kinetic;
+            const int n = a.p.req.particles;
+            std::vector<float> pos((size_t)n * 3), vel((size_t)n * 3);
+            std::vector<int32_t> sed(n);
+            sys_.get_particles(a.scene, pos.data(), vel.data(), nullptr, sed.data());
+            uint64_t h = 0xCBF29CE484222325ULL;
+            h = fnv1a(h, pos.data(), pos.size() * 4);
+            h = fnv1a(h, vel.data(), vel.size() * 4);
+            h = fnv1a(h, sed.data(), sed.size() * 4);
+            r.state_hash = h;
+            sys_.destroy_scene(a.scene);
+            reserved_ -= a.bytes;
+            resident_particles_ -= a.p.req.particles;
+            done_.push_back(r);
+            stats_.completed += 1;
+            stats_.particle_steps += (double)a.p.req.particles * (double)a.p.req.steps;
+        }
+        active_.swap(keep);
+    }
+
+    sph_server_config cfg_;
+    System sys_;
+    Clock::time_point t0_;
+    std::deque<Pending> queue_;
+    std::vector<Active> active_;
+    std::vector<sph_result> done_;
+    int64_t next_ticket_ = 1;
+    int64_t reserved_ = 0;
+    int64_t resident_particles_ = 0;
+    int chunks_ = 0;
+    sph_server_stats stats_{};
+
+   public:
+    int chunks() const { return chunks_; }
+};
+
+}  // namespace sph
+
+struct sph_server {
+    sph::Server* srv;
+};
+
+namespace {
+
+template <class F>
+int serve_guard(F&& f) {
+    try {
+        f();
+        return SPH_OK;
+    } catch (const sph::Error& e) {
+        sph::set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        sph::set_last_error("host allocation failed");
+        return SPH_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        sph::set_last_error(e.what());
+        return SPH_ERR_INVALID;
+    }
+}
+
+sph::Server& srv(sph_server* s) {
+    if (!s || !s->srv) throw sph::Error(SPH_ERR_INVALID, "null server handle");
+    return *s->srv;
+}
+
+}  // namespace
+
+struct sph_system {
+    sph::System* sys;
+};
+
+extern "C" {
+
+SPH_API int sph_scene_from_request(sph_system* s, const sph_params* base, const sph_request* r, int* scene) {
+    return serve_guard([&] {
+        if (!s || !s->sys || !base || !r || !scene) throw sph::Error(SPH_ERR_INVALID, "null argument");
+        *scene = sph::scene_from_request(*s->sys, *base, *r);
+    });
+}
+
+SPH_API void sph_server_config_default(sph_server_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof *c);
+    c->tile = 512;
+    c->cell_mult = 0.5f;
+    c->chunk_steps = 16;
+    c->hbm_budget = (int64_t)120 << 30;
+    c->max_scenes = 4096;
+    sph_params_default(&c->base);
+}
+
+SPH_API int sph_server_create(const sph_server_config* cfg, sph_server** out) {
+    return serve_guard([&] {
+        if (!out) throw sph::Error(SPH_ERR_INVALID, "null output handle");
+        *out = nullptr;
+        sph_server_config c;
+        if (cfg)
+            c = *cfg;
+        else
+            sph_server_config_default(&c);
+        *out = new sph_server{new sph::Server(c)};
+    });
+}
+
+SPH_API int sph_server_destroy(sph_server* s) {
+    return serve_guard([&] {
+        if (!s) return;
+        delete s->srv;
+        delete s;
+    });
+}
+
+SPH_API int sph_server_submit(sph_server* s, const sph_request* r, int64_t* ticket) {
+    return serve_guard([&] {
+        if (!r) throw sph::Error(SPH_ERR_INVALID, "null request");
+        sph::Server& S = srv(s);
+        const int64_t t = S.submit(*r, S.now());
+        if (ticket) *ticket = t;
+    });
+}
+
+SPH_API int sph_server_poll(sph_server* s, sph_result* out, int cap, int* n_out, int* active) {
+    return serve_guard([&] {
+        sph::Server& S = srv(s);
+        const int left = S.poll();
+        auto& d = S.done();
+        int k = 0;
+        if (out && cap > 0) {
+            k = std::min<int>(cap, (int)d.size());
+            std::copy(d.begin(), d.begin() + k, out);
+            d.erase(d.begin(), d.begin() + k);
+        }
+        if (n_out) *n_out = k;
+        if (active) *active = left;
+    });
+}
+
+SPH_API int sph_server_run_trace(sph_server* s, const sph_request* reqs, int n, sph_result* results,
+                                 sph_server_stats* stats) {
+    return serve_guard([&] {
+        sph::Server& S = srv(s);
+        if (n < 0 || (n > 0 && (!reqs || !results))) throw sph::Error(SPH_ERR_INVALID, "bad trace arguments");
+        std::vector<int> order(n);
+        for (int i = 0; i < n; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return reqs[a].arrival_s < reqs[b].arrival_s; });
+        S.done().clear();
+        S.stats() = sph_server_stats{};
+        S.restart_clock();
+        std::vector<int64_t> ticket_of(n);
+        for (int k = 0; k < n; ++k) ticket_of[order[k]] = S.submit(reqs[order[k]], reqs[order[k]].arrival_s);
+        const int chunks0 = S.chunks();
+        for (;;) {
+            const int left = S.poll();
+            if (left == 0) break;
+            double next;
+            if (S.idle_until_arrival(&next)) {
+                const double wait = next - S.now();
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
+            }
+        }
+        std::vector<sph_result>& d = S.done();
+        std::vector<double> lat;
+        double first = 1e300, last = 0.0;
+        for (const sph_result& r : d) {
+            lat.push_back(r.done_s - r.arrival_s);
+            first = std::min(first, r.arrival_s);
+            last = std::max(last, r.done_s);
+        }
+        for (int i = 0; i < n; ++i) {
+            auto it = std::find_if(d.begin(), d.end(), [&](const sph_result& r) { return r.ticket == ticket_of[i]; });
+            if (it == d.end()) throw sph::Error(SPH_ERR_STATE, "a request did not complete");
+            results[i] = *it;
+        }
+        std::sort(lat.begin(), lat.end());
+        sph_server_stats& st = S.stats();
+        if (!lat.empty()) {
+            auto rank = [&](double q) {
+                size_t k = (size_t)std::ceil(q * (double)lat.size());
+                return lat[std::min(lat.size() - 1, k > 0 ? k - 1 : 0)];
+            };
+            st.p50_s = rank(0.50);
+            st.p99_s = rank(0.99);
+            st.max_s = lat.back();
+            st.wall_s = last - first;
+            st.throughput = st.wall_s > 0 ? st.particle_steps / st.wall_s : 0.0;
+        }
+        st.chunks = S.chunks() - chunks0;
+        if (stats) *stats = st;
+        d.clear();
+    });
+}
+
+}  // extern "C"

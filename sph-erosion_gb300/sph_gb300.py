@@ -67,6 +67,34 @@ class SystemConfig(C.Structure):
     ]
 
 
+class Request(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("particles", C.c_int32), ("terrain_side", C.c_int32), ("steps", C.c_int32),
+                ("coverage", C.c_float), ("amplitude", C.c_float), ("arrival_s", C.c_double)]
+
+
+class Result(C.Structure):
+    _fields_ = [("ticket", C.c_int64), ("seed", C.c_uint64), ("particles", C.c_int32), ("steps", C.c_int32),
+                ("arrival_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
+                ("total_units", C.c_int64), ("sediment_units", C.c_int64), ("nan_particles", C.c_int32),
+                ("pad", C.c_int32), ("kinetic", C.c_double), ("state_hash", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("wall_s", C.c_double), ("particle_steps", C.c_double),
+                ("throughput", C.c_double), ("p50_s", C.c_double), ("p99_s", C.c_double), ("max_s", C.c_double),
+                ("peak_bytes", C.c_int64), ("peak_active", C.c_int32), ("chunks", C.c_int32),
+                ("peak_particles", C.c_int64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("tile", C.c_int), ("cell_mult", C.c_float), ("chunk_steps", C.c_int),
+                ("hbm_budget", C.c_int64), ("max_active_particles", C.c_int64), ("max_scenes", C.c_int),
+                ("base", Params)]
+
+
 _lib = None
 SIGNATURES = {
     "sph_last_error": (C.c_char_p, []),
@@ -101,7 +129,83 @@ SIGNATURES = {
     "sph_scene_neighbour_counts": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "sph_scene_grid_dims": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "sph_density_static": (C.c_int, [C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sph_scene_from_request": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Request), C.POINTER(C.c_int)]),
+    "sph_server_config_default": (None, [C.POINTER(ServerConfig)]),
+    "sph_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "sph_server_destroy": (C.c_int, [C.c_void_p]),
+    "sph_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
+    "sph_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sph_server_run_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(ServerStats)]),
 }
+
+
+def requests_array(reqs):
+    """A ctypes array of Request from dicts or Request objects."""
+    arr = (Request * len(reqs))()
+    for i, r in enumerate(reqs):
+        if isinstance(r, Request):
+            arr[i] = r
+        else:
+            arr[i] = Request(int(r["seed"]), int(r["particles"]), int(r["terrain_side"]), int(r.get("steps", 0)),
+                             float(r.get("coverage", 0.0)), float(r.get("amplitude", 0.0)),
+                             float(r.get("arrival_s", 0.0)))
+    return arr
+
+
+class Server:
+    """Continuous-batching request server (include/sph_erosion.h)."""
+
+    def __init__(self, base: Params = None, tile=512, cell_mult=0.5, chunk_steps=16, hbm_budget=0,
+                 max_active_particles=0, max_scenes=0, device=0):
+        cfg = ServerConfig()
+        lib().sph_server_config_default(C.byref(cfg))
+        cfg.device, cfg.tile, cfg.cell_mult, cfg.chunk_steps = device, tile, cell_mult, chunk_steps
+        if hbm_budget:
+            cfg.hbm_budget = hbm_budget
+        cfg.max_active_particles = max_active_particles
+        if max_scenes:
+            cfg.max_scenes = max_scenes
+        if base is not None:
+            cfg.base = base
+        h = C.c_void_p()
+        _ck(lib().sph_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().sph_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run_trace(self, reqs):
+        arr = requests_array(reqs)
+        res = (Result * len(arr))()
+        st = ServerStats()
+        _ck(lib().sph_server_run_trace(self.h, arr, len(arr), res, C.byref(st)))
+        return list(res), st.as_dict()
+
+    def submit(self, req) -> int:
+        arr = requests_array([req])
+        t = C.c_int64()
+        _ck(lib().sph_server_submit(self.h, C.byref(arr[0]), C.byref(t)))
+        return t.value
+
+    def poll(self, cap=64):
+        out = (Result * cap)()
+        n, active = C.c_int(), C.c_int()
+        _ck(lib().sph_server_poll(self.h, out, cap, C.byref(n), C.byref(active)))
+        return list(out[: n.value]), active.value
 
 
 def lib():
@@ -179,6 +283,12 @@ class System:
             self.close()
         except Exception:
             pass
+
+    def scene_from_request(self, base: Params, req) -> "Scene":
+        arr = requests_array([req])
+        sid = C.c_int()
+        _ck(lib().sph_scene_from_request(self.h, C.byref(base), C.byref(arr[0]), C.byref(sid)))
+        return Scene(self, sid.value)
 
     def scene(self, params: Params, capacity=0, terrain=(0, 0)) -> "Scene":
         sid = C.c_int()

@@ -72,6 +72,38 @@ def scaled_block(n, box_half=(0.5, 0.5, 0.5), amp=0.2):
     return lattice_block(nx, ny, nz, SPACING, lo, limit=n)
 
 
+def batched_requests(n_scenes=256, seed=1000, steps=0):
+    """The batched form: n_scenes independent scenes, scene i seeded with
+    seed + i; particle counts log-uniform in [2048, 131072]; heightmap side
+    uniform in {64, 128, 256, 512}; block coverage and terrain amplitude are
+    drawn by the library's recipe from each scene's seed."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(2048), np.log(131072), n_scenes)).astype(np.int64)
+    side = rng.choice([64, 128, 256, 512], n_scenes)
+    return [dict(seed=seed + i, particles=int(n[i]), terrain_side=int(side[i]), steps=steps)
+            for i in range(n_scenes)]
+
+
+def serving_trace(n_requests=10000, rate=200.0, seed=2000):
+    """The request stream: Poisson arrivals at `rate` per second (exponential
+    gaps), particle counts log-uniform in [4096, 262144], heightmap side
+    uniform in {128, 256, 512}, step counts uniform in [100, 2000]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    n = np.exp(rng.uniform(np.log(4096), np.log(262144), n_requests)).astype(np.int64)
+    side = rng.choice([128, 256, 512], n_requests)
+    steps = rng.integers(100, 2001, n_requests)
+    return [dict(seed=seed + i, particles=int(n[i]), terrain_side=int(side[i]), steps=int(steps[i]),
+                 arrival_s=float(t[i])) for i in range(n_requests)]
+
+
+def base_params(cell_mult=0.5, flags=0):
+    """Physical constants shared by every seeded scene."""
+    import sph_gb300 as S
+
+    return S.default_params(**dict(PHYS, cell_mult=cell_mult, flags=flags))
+
+
 def build_scene(system, spec, flags=0, capacity=0):
     """Create a scene of `spec` in a sph_gb300.System."""
     import sph_gb300 as S
