@@ -174,6 +174,17 @@ SPH_API int sph_scene_gen_terrain(sph_system* s, int scene, uint64_t seed, int o
 /* Current heights (base + delta) and the int64 deltas (either may be NULL). */
 SPH_API int sph_scene_get_terrain(sph_system* s, int scene, float* heights, int64_t* delta);
 SPH_API int sph_scene_terrain_dims(sph_system* s, int scene, int* w, int* d);
+/* Grid::UpdateGrid + genIndices (grid.h:118-176) on the GPU for the
+ * reference's 512 x 512 8-bit heightfield (x-major, map[512 * x + z]):
+ * verts gets 6 floats (x, y, z, normal) per (x, z) for x < dimx, z < dimz
+ * (z-major); indices gets 6 (dimx - 1)(dimz - 1) triangle corners.  Either
+ * output may be NULL; *n_indices receives the index count. */
+SPH_API int sph_terrain_mesh_u8(const unsigned char* map512, int dimx, int dimy, int dimz, float* verts,
+                                unsigned* indices, int64_t index_cap, int64_t* n_indices);
+/* The same surface mesh for a scene's current (eroded) heights, in world
+ * units: tw * td vertices (x, y, z, normal), z-major, and
+ * 6 (tw - 1)(td - 1) indices.  The front end's per-frame terrain redraw. */
+SPH_API int sph_scene_terrain_mesh(sph_system* s, int scene, float* verts, unsigned* indices);
 
 /* ---- inspection for parity checks ---------------------------------------- */
 /* Cell key of each particle and the stable sorted order (ids), as the next

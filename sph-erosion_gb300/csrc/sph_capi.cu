@@ -8,10 +8,6 @@
 #include "../../include/sph_erosion.h"
 #include "sph_engine.h"
 
-struct sph_system {
-    sph::System* sys;
-};
-
 namespace {
 
 thread_local std::string g_err;

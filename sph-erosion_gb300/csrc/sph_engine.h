@@ -178,6 +178,21 @@ void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, floa
 // Sets the calling thread's sph_last_error() message (sph_capi.cu).
 void set_last_error(const std::string& msg);
 
+// Terrain meshes (sph_mesh.cu).
+void mesh_u8(const unsigned char* map_host, int dimx, int dimy, int dimz, float* verts, unsigned* idx,
+             int64_t idx_cap, int64_t* n_idx);
+void mesh_scene(System& sys, int scene, float* verts, unsigned* idx);
+int scene_from_request(System& sys, const sph_params& base, const sph_request& r);
+
+}  // namespace sph
+
+// The opaque handle of include/sph_erosion.h.
+struct sph_system {
+    sph::System* sys;
+};
+
+namespace sph {
+
 // Host FP32 constants of a scene (sph_engine.cu): exposed for inspection.
 float smax_for(float h);
 float coincidence_threshold();

@@ -259,10 +259,6 @@ sph::Server& srv(sph_server* s) {
 
 }  // namespace
 
-struct sph_system {
-    sph::System* sys;
-};
-
 extern "C" {
 
 SPH_API int sph_scene_from_request(sph_system* s, const sph_params* base, const sph_request* r, int* scene) {
