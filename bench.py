@@ -180,10 +180,12 @@ def run_ours(args, spec, config):
     spec = dict(spec, params=dict(spec["params"], cell_mult=args.cell_mult))
     sc = W.build_scene(sysm, spec)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    # warm-up
+    # warm-up, then the autotuner picks tile and cell size from this state
+    # (each trial restarts from a snapshot; the state is restored after)
     for _ in range(args.warmup):
         sysm.step(1)
     sysm.sync()
+    tuned = sysm.autotune(8) if args.autotune else None
     torch.cuda.synchronize()
     # timed: K steps, each bracketed by CUDA events on the library stream,
     # an L2 flush before each
@@ -242,6 +244,9 @@ def run_ours(args, spec, config):
         "stages_ms": {name: float(v) for name, v in zip(S.STAGES, stages)},
         "clocks": clk.summary(),
         "mass_units_total": int(d["total_units"]),
+        "diag_fp64": {"kinetic": d["kinetic"], "potential": d["potential"], "momentum": d["momentum"],
+                      "nan_particles": d["nan_particles"]},
+        "tuned": tuned,
     }
     print(json.dumps(line), flush=True)
 
@@ -321,7 +326,10 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plain_1m", choices=["plain_1m", "plain_small", "batched", "serving"])
+    ap.add_argument("--workload", default="plain_1m",
+                    choices=["plain_1m", "plain_small", "batched", "serving", "skew"])
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep --tile/--cell-mult instead of autotuning them")
     ap.add_argument("--tile", type=int, default=512)
     ap.add_argument("--cell-mult", type=float, default=0.5)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
@@ -337,7 +345,7 @@ def main():
         cfg = {"h": W.H, "dt": W.PHYS["dt"], "erosion": True, "tile": args.tile, "cell_mult": args.cell_mult}
         (run_batched if args.workload == "batched" else run_serving)(args, cfg)
         return
-    spec = W.plain_1m() if args.workload != "plain_small" else W.plain_small()
+    spec = {"plain_small": W.plain_small, "skew": W.skew_rain}.get(args.workload, W.plain_1m)()
     t = spec.get("terrain")
     config = {"workload": spec["name"], "particles": spec["n"],
               "terrain": f"{t['w']}x{t['d']} fBm {t['octaves']} oct amp {t['amplitude']}" if t else None,

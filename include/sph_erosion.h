@@ -133,6 +133,26 @@ SPH_API int sph_system_profile_stages(sph_system* s, int nsteps, float* ms);
 /* Bytes of device memory the system holds. */
 SPH_API int sph_system_memory(sph_system* s, int64_t* bytes);
 
+/* Autotuner (no counterpart in the reference).  Times `steps` steps of the
+ * system's current scenes under each candidate of particles per work tile
+ * (block size: 128, 256, 512) and grid cell edge (cell_mult 1 or 0.5, i.e.
+ * 27 cells of h or 125 cells of h/2 around a particle), each trial starting
+ * from the same snapshot of every scene's state, then keeps the fastest and
+ * restores the state.  One particle per thread (32 per warp) and a re-sort
+ * every step are fixed: the exact neighbour sets need the current sort.
+ * In fast mode the cell size changes the order in which neighbours are
+ * summed, hence the last bits of the results (within the 1e-4 parity bar). */
+typedef struct sph_tune_result {
+    int tile;
+    float cell_mult;
+    float ms_per_step;
+    int n_tried;
+    int tiles[8];
+    float cell_mults[8];
+    float ms[8];
+} sph_tune_result;
+SPH_API int sph_system_autotune(sph_system* s, int steps, sph_tune_result* out);
+
 /* ---- scenes (one FluidSystemSPH + Grid each) ------------------------------ */
 /* FluidSystemSPH() (fluid_system.h:69-72): a scene with no particles.
  * terrain_w/terrain_d = 0 for no terrain; capacity is a hint. */
@@ -167,8 +187,10 @@ SPH_API int sph_scene_diag(sph_system* s, int scene, sph_diag* out);
 /* LoadHeightfield generalised to any size and FP32 metres above the box floor
  * (grid.h:98-102); resets the int64 erosion deltas to zero. */
 SPH_API int sph_scene_set_terrain(sph_system* s, int scene, int w, int d, const float* heights);
-/* Seeded fBm value noise (kind 0) or ridged fBm (kind 1) of the given
- * octaves, amplitude, lacunarity and gain (the repository's own generator). */
+/* Seeded fBm value noise (kind 0), ridged fBm (kind 1) or carved valleys
+ * (kind 2: amplitude minus the ridged field, sharp valleys cut into a
+ * plateau) of the given octaves, amplitude, lacunarity and gain (the
+ * repository's own generator). */
 SPH_API int sph_scene_gen_terrain(sph_system* s, int scene, uint64_t seed, int octaves, float amplitude,
                           float lacunarity, float gain, int kind);
 /* Current heights (base + delta) and the int64 deltas (either may be NULL). */

@@ -294,7 +294,7 @@ void oracle_fbm(uint64_t seed, int w, int d, int octaves, float amplitude, float
             for (o = 0; o < octaves; o++) {
                 uint64_t oseed = splitmix64(seed + (uint64_t)o);
                 double nv = value_noise(oseed, u * freq, v * freq);
-                if (kind == 1) {
+                if (kind != 0) {
                     double r = 1.0 - fabs(2.0 * nv - 1.0);
                     nv = r * r;
                 }
@@ -302,7 +302,8 @@ void oracle_fbm(uint64_t seed, int w, int d, int octaves, float amplitude, float
                 a *= (double)gain;
                 freq *= (double)lacunarity;
             }
-            out[(size_t)iz * (size_t)w + (size_t)ix] = (float)((double)amplitude * (sum / norm));
+            out[(size_t)iz * (size_t)w + (size_t)ix] =
+                (float)((double)amplitude * (kind == 2 ? 1.0 - sum / norm : sum / norm));
         }
     }
 }

@@ -128,6 +128,13 @@ int sph_system_profile_stages(sph_system* s, int nsteps, float* ms) {
     });
 }
 
+int sph_system_autotune(sph_system* s, int steps, sph_tune_result* out) {
+    return guard([&] {
+        need(out, "out");
+        sys(s).autotune(steps, out);
+    });
+}
+
 int sph_system_memory(sph_system* s, int64_t* bytes) {
     return guard([&] {
         need(bytes, "bytes");
@@ -241,7 +248,7 @@ int sph_scene_gen_terrain(sph_system* s, int scene, uint64_t seed, int octaves, 
                           float gain, int kind) {
     return guard([&] {
         if (octaves < 1 || octaves > 16) throw sph::Error(SPH_ERR_INVALID, "octaves must be in [1, 16]");
-        if (kind != 0 && kind != 1) throw sph::Error(SPH_ERR_INVALID, "kind must be 0 or 1");
+        if (kind < 0 || kind > 2) throw sph::Error(SPH_ERR_INVALID, "kind must be 0, 1 or 2");
         sys(s).gen_terrain(scene, seed, octaves, amplitude, lacunarity, gain, kind);
     });
 }

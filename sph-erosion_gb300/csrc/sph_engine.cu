@@ -1072,6 +1072,101 @@ void System::neighbour_counts(int id, int32_t* out) {
     SPH_CK(cudaStreamSynchronize(st_));
 }
 
+// ---- autotuner ------------------------------------------------------------------
+void System::autotune(int steps, sph_tune_result* out) {
+    if (steps <= 0) throw Error(SPH_ERR_INVALID, "autotune needs steps > 0");
+    std::memset(out, 0, sizeof *out);
+    if (work_dirty_) rebuild_work();
+    SPH_CK(cudaStreamSynchronize(st_));
+    // snapshot of every scene's evolving state: particles (whole arena, so
+    // ranges stay valid), terrain deltas and heights, step budgets
+    const int64_t np = pos_.n, nt = tbase_.n;
+    DevBuf<float4> spos, svel;
+    DevBuf<int32_t> snb;
+    DevBuf<long long> sdel;
+    DevBuf<float> shgt;
+    spos.resize(np, false, st_);
+    svel.resize(np, false, st_);
+    snb.resize(np, false, st_);
+    sdel.resize(nt, false, st_);
+    shgt.resize(nt, false, st_);
+    auto copy = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes) SPH_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st_));
+    };
+    copy(spos.p, pos_.p, np * 16);
+    copy(svel.p, vel_.p, np * 16);
+    copy(snb.p, nbid_.p, np * 4);
+    copy(sdel.p, tdelta_.p, nt * 8);
+    copy(shgt.p, theight_.p, nt * 4);
+    std::vector<int> steps0;
+    for (const Scene& sc : scenes_) steps0.push_back(sc.steps);
+    SPH_CK(cudaStreamSynchronize(st_));
+    auto restore = [&]() {
+        copy(pos_.p, spos.p, np * 16);
+        copy(vel_.p, svel.p, np * 16);
+        copy(nbid_.p, snb.p, np * 4);
+        copy(tdelta_.p, sdel.p, nt * 8);
+        copy(theight_.p, shgt.p, nt * 4);
+        for (size_t i = 0; i < scenes_.size(); ++i)
+            if (scenes_[i].live) set_steps((int)i, steps0[i]);
+        SPH_CK(cudaStreamSynchronize(st_));
+    };
+    auto apply = [&](int tile, float cm) {
+        if (cfg_.tile != tile) {
+            cfg_.tile = tile;
+            work_dirty_ = true;
+            drop_graph();
+        }
+        for (size_t i = 0; i < scenes_.size(); ++i) {
+            if (!scenes_[i].live || scenes_[i].prm.cell_mult == cm) continue;
+            sph_params p = scenes_[i].prm;
+            p.cell_mult = cm;
+            set_params((int)i, p);
+        }
+        if (pos_.n != np || tbase_.n != nt) throw Error(SPH_ERR_STATE, "arena changed while tuning");
+    };
+    auto free_snapshot = [&]() {
+        spos.release();
+        svel.release();
+        snb.release();
+        sdel.release();
+        shgt.release();
+    };
+    const int tiles[3] = {128, 256, 512};
+    const float cms[2] = {1.0f, 0.5f};
+    float best = 1e30f;
+    int bt = cfg_.tile;
+    float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;
+    try {
+        for (float cm : cms)
+            for (int tile : tiles) {
+                apply(tile, cm);
+                step(2);  // warm-up: graphs captured, caches primed
+                SPH_CK(cudaStreamSynchronize(st_));
+                const float ms = time_steps(steps) / (float)steps;
+                restore();
+                const int k = out->n_tried++;
+                out->tiles[k] = tile;
+                out->cell_mults[k] = cm;
+                out->ms[k] = ms;
+                if (ms < best) {
+                    best = ms;
+                    bt = tile;
+                    bc = cm;
+                }
+            }
+        apply(bt, bc);
+        restore();
+    } catch (...) {
+        free_snapshot();
+        throw;
+    }
+    free_snapshot();
+    out->tile = bt;
+    out->cell_mult = bc;
+    out->ms_per_step = best;
+}
+
 template struct DevBuf<float4>;
 template struct DevBuf<float>;
 template struct DevBuf<uint32_t>;

@@ -94,6 +94,7 @@ class System {
 
     void step(int nsteps);
     void sync();
+    void autotune(int steps, sph_tune_result* out);
     float time_steps(int nsteps);
     void profile_stages(int nsteps, float* ms);
     int64_t memory_bytes() const;

@@ -8,7 +8,8 @@
 //   vertex (ix, iz) samples u = ix/(w-1), v = iz/(d-1) at frequency 4 * lac^o;
 //   ridged variant per octave: (1 - |2n - 1|)^2;
 //   height = amplitude * sum_o gain^o n_o / sum_o gain^o, in double, rounded once
-//   to float.
+//   to float; the carved variant (kind 2) is amplitude * (1 - ridged sum /
+//   norm): the ridges become sharp valleys cut into a plateau.
 #include <cmath>
 #include <cstdint>
 #include <thread>
@@ -63,7 +64,7 @@ void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, floa
                 double freq = 4.0, a = 1.0, sum = 0.0;
                 for (int o = 0; o < octaves; ++o) {
                     double n = noise2(oseed[o], u * freq, v * freq);
-                    if (kind == 1) {
+                    if (kind != 0) {
                         const double r = 1.0 - std::fabs(2.0 * n - 1.0);
                         n = r * r;
                     }
@@ -71,7 +72,8 @@ void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, floa
                     a *= (double)gain;
                     freq *= (double)lacunarity;
                 }
-                out[(size_t)iz * (size_t)w + (size_t)ix] = (float)((double)amplitude * (sum / norm));
+                const double f = kind == 2 ? 1.0 - sum / norm : sum / norm;
+                out[(size_t)iz * (size_t)w + (size_t)ix] = (float)((double)amplitude * f);
             }
     };
     const int64_t work = (int64_t)w * d * (octaves > 0 ? octaves : 1);

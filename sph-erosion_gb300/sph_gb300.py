@@ -95,8 +95,18 @@ class ServerConfig(C.Structure):
                 ("base", Params)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("tile", C.c_int), ("cell_mult", C.c_float), ("ms_per_step", C.c_float), ("n_tried", C.c_int),
+                ("tiles", C.c_int * 8), ("cell_mults", C.c_float * 8), ("ms", C.c_float * 8)]
+
+    def as_dict(self):
+        return {"tile": self.tile, "cell_mult": self.cell_mult, "ms_per_step": self.ms_per_step,
+                "tried": [(self.tiles[i], self.cell_mults[i], self.ms[i]) for i in range(self.n_tried)]}
+
+
 _lib = None
 SIGNATURES = {
+    "sph_system_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(TuneResult)]),
     "sph_last_error": (C.c_char_p, []),
     "sph_params_default": (None, [C.POINTER(Params)]),
     "sph_system_config_default": (None, [C.POINTER(SystemConfig)]),
@@ -311,6 +321,11 @@ class System:
         out = np.zeros(8, np.float32)
         _ck(lib().sph_system_profile_stages(self.h, int(n), _p(out)))
         return out
+
+    def autotune(self, steps=8) -> dict:
+        r = TuneResult()
+        _ck(lib().sph_system_autotune(self.h, int(steps), C.byref(r)))
+        return r.as_dict()
 
     def memory(self) -> int:
         b = C.c_int64()

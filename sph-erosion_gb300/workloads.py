@@ -72,6 +72,26 @@ def scaled_block(n, box_half=(0.5, 0.5, 0.5), amp=0.2):
     return lattice_block(nx, ny, nz, SPACING, lo, limit=n)
 
 
+def skew_rain(n=8388608, seed=5, terrain_side=4096):
+    """Skewed-occupancy stress: n particles released as rainfall (x, z uniform
+    over the box floor, y uniform in the top 10% of the box height) over a
+    terrain_side^2 carved-valley terrain (inverted ridged fBm, 6 octaves,
+    amplitude 0.5), at rest.  The box (16 x 2 x 16 m) makes the rain layer's
+    mean density about 1.3x the rest density; the rain then pools in the
+    valleys into very uneven cell occupancy."""
+    box_half = (8.0, 1.0, 8.0)
+    rng = np.random.default_rng(seed)
+    pos = np.empty((n, 3), np.float32)
+    pos[:, 0] = rng.uniform(-box_half[0] + SPACING / 2, box_half[0] - SPACING / 2, n)
+    pos[:, 2] = rng.uniform(-box_half[2] + SPACING / 2, box_half[2] - SPACING / 2, n)
+    top = box_half[1]
+    pos[:, 1] = rng.uniform(top - 0.1 * 2 * box_half[1], top - SPACING / 2, n)
+    prm = dict(PHYS, box_half=box_half)
+    return dict(name="skew_rain", params=prm, pos=pos, n=n,
+                terrain=dict(w=terrain_side, d=terrain_side, seed=seed, octaves=6, amplitude=0.5, lacunarity=2.0,
+                             gain=0.5, kind=2))
+
+
 def batched_requests(n_scenes=256, seed=1000, steps=0):
     """The batched form: n_scenes independent scenes, scene i seeded with
     seed + i; particle counts log-uniform in [2048, 131072]; heightmap side

@@ -101,6 +101,38 @@ def test_server_admission_respects_budget():
     assert before > 0
 
 
+def test_autotune_restores_state_and_applies_choice():
+    """After tuning, the system continues from the untouched state with the
+    chosen tile and cell size: identical to a fresh run with that choice."""
+    reqs = SMALL[:3]
+    with S.System(tile=256) as sysm:
+        scenes = [sysm.scene_from_request(W.base_params(1.0), r) for r in reqs]
+        sysm.step(5)
+        before = [_state(sc) for sc in scenes]
+        tuned = sysm.autotune(4)
+        assert len(tuned["tried"]) == 6 and tuned["tile"] in (128, 256, 512)
+        assert tuned["ms_per_step"] == min(t[2] for t in tuned["tried"])
+        for sc, st in zip(scenes, before):
+            for a, b in zip(_state(sc), st):
+                assert np.array_equal(a, b)
+            assert sc.params().cell_mult == tuned["cell_mult"]
+        sysm.step(10)
+        after = [_state(sc) for sc in scenes]
+    # the same history without tuning: 5 steps, switch the cell size, 10 steps
+    # (the tile size never changes results)
+    with S.System(tile=256) as ref:
+        rs = [ref.scene_from_request(W.base_params(1.0), r) for r in reqs]
+        ref.step(5)
+        for sc in rs:
+            p = sc.params()
+            p.cell_mult = tuned["cell_mult"]
+            sc.set_params(p)
+        ref.step(10)
+        for sc, st in zip(rs, after):
+            for a, b in zip(_state(sc), st):
+                assert np.array_equal(a, b)
+
+
 def test_server_submit_poll():
     with S.Server(W.base_params(), chunk_steps=8) as srv:
         tickets = [srv.submit(r) for r in SMALL[:3]]
