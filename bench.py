@@ -158,6 +158,18 @@ def run_reference(args, spec, config):
     print(json.dumps(line), flush=True)
 
 
+def traversal(scene, step_ms):
+    """Neighbour-search counters at the end of the run: per particle, the
+    candidates each of the two neighbour passes tests and the in-range pairs
+    it evaluates; pair tests per second over the whole step."""
+    t = scene.traversal_stats()
+    n = max(t["particles"], 1)
+    return {"candidates_per_particle": t["candidates"] / n, "in_range_per_particle": t["in_range"] / n,
+            "rows_per_particle": t["rows"] / n, "pair_tests_per_s": 2 * t["candidates"] / (step_ms * 1e-3),
+            "in_range_pairs_per_s": 2 * t["in_range"] / (step_ms * 1e-3),
+            "reference_pair_tests_per_step": 3 * n * n}
+
+
 def flush_l2(buf):
     buf.zero_()
 
@@ -247,6 +259,7 @@ def run_ours(args, spec, config):
         "diag_fp64": {"kinetic": d["kinetic"], "potential": d["potential"], "momentum": d["momentum"],
                       "nan_particles": d["nan_particles"]},
         "tuned": tuned,
+        "traversal": traversal(sc, step_ms),
     }
     print(json.dumps(line), flush=True)
 

@@ -107,6 +107,8 @@ typedef struct sph_system_config {
     int max_scenes;
     int tile;                 /* particles per work tile: 128, 256 or 512 (0 = 256) */
     int graph_steps;          /* steps per captured CUDA graph (0 = no graphs) */
+    int variant;              /* kernel variant bits, picked by the autotuner:
+                                 1 = density pass over compacted neighbour lists */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;
 
@@ -135,20 +137,23 @@ SPH_API int sph_system_memory(sph_system* s, int64_t* bytes);
 
 /* Autotuner (no counterpart in the reference).  Times `steps` steps of the
  * system's current scenes under each candidate of particles per work tile
- * (block size: 128, 256, 512) and grid cell edge (cell_mult 1 or 0.5, i.e.
- * 27 cells of h or 125 cells of h/2 around a particle), each trial starting
- * from the same snapshot of every scene's state, then keeps the fastest and
- * restores the state.  One particle per thread (32 per warp) and a re-sort
- * every step are fixed: the exact neighbour sets need the current sort.
- * In fast mode the cell size changes the order in which neighbours are
- * summed, hence the last bits of the results (within the 1e-4 parity bar). */
+ * (block size 256 or 512), grid cell edge (cell_mult 1 or 0.5, i.e. 27 cells
+ * of h or 125 cells of h/2 around a particle) and density-pass variant
+ * (direct or compacted lists), each trial starting from the same snapshot of
+ * every scene's state, then keeps the fastest and restores the state.  One
+ * particle per thread (32 per warp) and a re-sort every step are fixed: the
+ * exact neighbour sets need the current sort.  In fast mode the cell size
+ * changes the order in which neighbours are summed, hence the last bits of
+ * the results (within the 1e-4 parity bar). */
 typedef struct sph_tune_result {
     int tile;
     float cell_mult;
+    int variant;
     float ms_per_step;
     int n_tried;
     int tiles[8];
     float cell_mults[8];
+    int variants[8];
     float ms[8];
 } sph_tune_result;
 SPH_API int sph_system_autotune(sph_system* s, int steps, sph_tune_result* out);
@@ -217,6 +222,10 @@ SPH_API int sph_scene_debug_sort(sph_system* s, int scene, uint32_t* keys_by_id,
 SPH_API int sph_scene_neighbour_counts(sph_system* s, int scene, int32_t* counts_by_id);
 /* Grid dims used by the sort: nx ny nz nkeys. */
 SPH_API int sph_scene_grid_dims(sph_system* s, int scene, int* dims4);
+/* Counters of the neighbour search the next step would run, from the current
+ * positions: out4 = particles, cell rows visited, candidates tested, in-range
+ * pairs (self included).  The reference tests n^2 pairs per pass. */
+SPH_API int sph_scene_traversal_stats(sph_system* s, int scene, int64_t* out4);
 
 /* ---- seeded scenes, batching and the request server -----------------------
  * No counterpart in the reference (a single interactive scene).  A request

@@ -128,6 +128,13 @@ int sph_system_profile_stages(sph_system* s, int nsteps, float* ms) {
     });
 }
 
+int sph_scene_traversal_stats(sph_system* s, int scene, int64_t* out4) {
+    return guard([&] {
+        need(out4, "out4");
+        sys(s).traversal_stats(scene, out4);
+    });
+}
+
 int sph_system_autotune(sph_system* s, int steps, sph_tune_result* out) {
     return guard([&] {
         need(out, "out");

@@ -201,7 +201,7 @@ System::~System() {
     counts_.release(); offsets_.release(); chunk_.release(); tab_.release();
     tbase_.release(); theight_.release(); tdelta_.release();
     dscenes_.release(); steps_.release(); ptiles_.release(); ctiles_.release(); ttiles_.release();
-    nwork_.release(); slist_.release(); status_.release(); scratch_i_.release();
+    nwork_.release(); slist_.release(); status_.release(); scratch_i_.release(); stage_.release();
     diag_part_.release(); diag_i_.release(); diag_nan_.release();
     if (st_) cudaStreamDestroy(st_);
 }
@@ -656,31 +656,21 @@ void System::get_particles(int id, float* pos3, float* vel3, float* density, int
     SPH_CK(cudaStreamSynchronize(st_));
     check_status();
     const int n = sc.n;
-    std::vector<float4> hp(n), hv(n), hd;
     if (n == 0) return;
-    SPH_CK(cudaMemcpyAsync(hp.data(), pos_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
-    SPH_CK(cudaMemcpyAsync(hv.data(), vel_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
-    if (density) {
-        hd.resize(n);
-        SPH_CK(cudaMemcpyAsync(hd.data(), dyn_.p + sc.p_off, (size_t)n * 16, cudaMemcpyDeviceToHost, st_));
-    }
+    // gather into id order on the device, then copy only what was asked for
+    if (stage_.n < (int64_t)8 * n) stage_.resize((int64_t)8 * n, false, st_);
+    float* d_pos = stage_.p;
+    float* d_vel = stage_.p + (size_t)3 * n;
+    float* d_den = stage_.p + (size_t)6 * n;
+    int32_t* d_sed = reinterpret_cast<int32_t*>(stage_.p + (size_t)7 * n);
+    launch_gather_by_id(pos_.p, vel_.p, dyn_.p, (int)sc.p_off, n, pos3 ? d_pos : nullptr, vel3 ? d_vel : nullptr,
+                        density ? d_den : nullptr, sed ? d_sed : nullptr, st_);
+    SPH_CK(cudaGetLastError());
+    if (pos3) SPH_CK(cudaMemcpyAsync(pos3, d_pos, (size_t)n * 12, cudaMemcpyDeviceToHost, st_));
+    if (vel3) SPH_CK(cudaMemcpyAsync(vel3, d_vel, (size_t)n * 12, cudaMemcpyDeviceToHost, st_));
+    if (density) SPH_CK(cudaMemcpyAsync(density, d_den, (size_t)n * 4, cudaMemcpyDeviceToHost, st_));
+    if (sed) SPH_CK(cudaMemcpyAsync(sed, d_sed, (size_t)n * 4, cudaMemcpyDeviceToHost, st_));
     SPH_CK(cudaStreamSynchronize(st_));
-    for (int p = 0; p < n; ++p) {
-        const int i = float_to_bits(hp[p].w);
-        if (i < 0 || i >= n) throw Error(SPH_ERR_DEVICE, "corrupt particle id");
-        if (pos3) {
-            pos3[3 * i] = hp[p].x;
-            pos3[3 * i + 1] = hp[p].y;
-            pos3[3 * i + 2] = hp[p].z;
-        }
-        if (vel3) {
-            vel3[3 * i] = hv[p].x;
-            vel3[3 * i + 1] = hv[p].y;
-            vel3[3 * i + 2] = hv[p].z;
-        }
-        if (density) density[i] = hd[p].x;
-        if (sed) sed[i] = float_to_bits(hv[p].w);
-    }
 }
 
 void System::get_records(int id, float* rec27, int* nbid, int32_t* sed) {
@@ -897,6 +887,7 @@ LaunchShape System::shape() const {
     s.grid_p = n_ptiles_;
     s.grid_c = n_ctiles_;
     s.grid_t = n_ttiles_;
+    s.variant = cfg_.variant;
     return s;
 }
 
@@ -1059,6 +1050,26 @@ void System::debug_sort(int id, uint32_t* keys_by_id, int32_t* sorted_ids) {
     }
 }
 
+void System::traversal_stats(int id, int64_t* out4) {
+    Scene& sc = scene(id);
+    if (work_dirty_) rebuild_work();
+    out4[0] = sc.n;
+    out4[1] = out4[2] = out4[3] = 0;
+    if (sc.n == 0) return;
+    const DevArrays a = arrays();
+    enqueue_sort(a, shape());
+    if (diag_i_.n < 4) diag_i_.resize(4, false, st_);
+    SPH_CK(cudaMemsetAsync(diag_i_.p, 0, 4 * sizeof(long long), st_));
+    launch_traversal_stats(a, id, reinterpret_cast<unsigned long long*>(diag_i_.p), st_);
+    SPH_CK(cudaGetLastError());
+    long long h[3];
+    SPH_CK(cudaMemcpyAsync(h, diag_i_.p, sizeof h, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaStreamSynchronize(st_));
+    out4[1] = h[0];
+    out4[2] = h[1];
+    out4[3] = h[2];
+}
+
 void System::neighbour_counts(int id, int32_t* out) {
     Scene& sc = scene(id);
     if (work_dirty_) rebuild_work();
@@ -1111,9 +1122,10 @@ void System::autotune(int steps, sph_tune_result* out) {
             if (scenes_[i].live) set_steps((int)i, steps0[i]);
         SPH_CK(cudaStreamSynchronize(st_));
     };
-    auto apply = [&](int tile, float cm) {
-        if (cfg_.tile != tile) {
+    auto apply = [&](int tile, float cm, int variant) {
+        if (cfg_.tile != tile || cfg_.variant != variant) {
             cfg_.tile = tile;
+            cfg_.variant = variant;
             work_dirty_ = true;
             drop_graph();
         }
@@ -1132,30 +1144,34 @@ void System::autotune(int steps, sph_tune_result* out) {
         sdel.release();
         shgt.release();
     };
-    const int tiles[3] = {128, 256, 512};
+    const int tiles[2] = {256, 512};
     const float cms[2] = {1.0f, 0.5f};
+    const int variants[2] = {0, 1};
     float best = 1e30f;
-    int bt = cfg_.tile;
+    int bt = cfg_.tile, bv = cfg_.variant;
     float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;
     try {
         for (float cm : cms)
-            for (int tile : tiles) {
-                apply(tile, cm);
-                step(2);  // warm-up: graphs captured, caches primed
-                SPH_CK(cudaStreamSynchronize(st_));
-                const float ms = time_steps(steps) / (float)steps;
-                restore();
-                const int k = out->n_tried++;
-                out->tiles[k] = tile;
-                out->cell_mults[k] = cm;
-                out->ms[k] = ms;
-                if (ms < best) {
-                    best = ms;
-                    bt = tile;
-                    bc = cm;
+            for (int variant : variants)
+                for (int tile : tiles) {
+                    apply(tile, cm, variant);
+                    step(2);  // warm-up: graphs captured, caches primed
+                    SPH_CK(cudaStreamSynchronize(st_));
+                    const float ms = time_steps(steps) / (float)steps;
+                    restore();
+                    const int k = out->n_tried++;
+                    out->tiles[k] = tile;
+                    out->cell_mults[k] = cm;
+                    out->variants[k] = variant;
+                    out->ms[k] = ms;
+                    if (ms < best) {
+                        best = ms;
+                        bt = tile;
+                        bc = cm;
+                        bv = variant;
+                    }
                 }
-            }
-        apply(bt, bc);
+        apply(bt, bc, bv);
         restore();
     } catch (...) {
         free_snapshot();
@@ -1164,6 +1180,7 @@ void System::autotune(int steps, sph_tune_result* out) {
     free_snapshot();
     out->tile = bt;
     out->cell_mult = bc;
+    out->variant = bv;
     out->ms_per_step = best;
 }
 

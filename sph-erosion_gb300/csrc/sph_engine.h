@@ -90,6 +90,7 @@ class System {
     void terrain_dims(int id, int* w, int* d) const;
     void debug_sort(int id, uint32_t* keys_by_id, int32_t* sorted_ids);
     void neighbour_counts(int id, int32_t* out);
+    void traversal_stats(int id, int64_t* out4);
     void grid_dims(int id, int* dims4) const;
 
     void step(int nsteps);
@@ -158,6 +159,7 @@ class System {
     DevBuf<int> slist_;
     DevBuf<unsigned> status_;
     DevBuf<int32_t> scratch_i_;
+    DevBuf<float> stage_;  // id-order readback staging (8 floats per particle)
     DevBuf<double> diag_part_;
     DevBuf<long long> diag_i_;
     DevBuf<int> diag_nan_;

@@ -273,7 +273,9 @@ __device__ __forceinline__ void force_pair(const SceneDev& S, ForceAcc& acc, flo
         gy = -t;
         gz = -t;
     } else {
-        float inv = fdv(1.0f, len);  // glm::normalize: r * (1 / sqrt(dot(r, r)))
+        // glm::normalize: r * (1 / sqrt(dot(r, r))); the correctly rounded
+        // reciprocal is the same value as the correctly rounded 1/len
+        float inv = __frcp_rn(len);
         gx = -fm(fm(fm(rx, inv), S.c_spiky), pw2);
         gy = -fm(fm(fm(ry, inv), S.c_spiky), pw2);
         gz = -fm(fm(fm(rz, inv), S.c_spiky), pw2);
@@ -533,7 +535,10 @@ __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
 
 // density: pass 1 (fluid_system.h:107-124), then the per-particle factors the
 // force pass reuses: P/rho^2 and m/rho.
-template <bool ORDERED>
+// LISTED: the in-range pairs are compacted (for_each_in_range_listed) instead
+// of evaluated inside the candidate loop; which one is faster depends on the
+// neighbour density, so the autotuner picks it.
+template <bool ORDERED, bool LISTED>
 __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
@@ -544,7 +549,7 @@ __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
         if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
         const int p = wk.start + threadIdx.x;
         const bool valid = p < S.p_off + S.n;
-        if (ORDERED && !valid) continue;
+        if ((ORDERED || !LISTED) && !valid) continue;
         const float4 xi = a.spos[valid ? p : S.p_off];
         float rho = 0.0f;
         if (ORDERED) {
@@ -553,9 +558,15 @@ __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
                 if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
             };
             if (!for_each_in_range_ordered(a, S, xi, term)) atomicOr(a.status, 1u);
-        } else {
-            // the density term is cheap: a direct traversal beats compaction
+        } else if (LISTED) {
+            const float4* sp = a.spos + S.p_off;
+            for_each_in_range_listed(a, S, valid, xi, list, [&](uint32_t j) {
+                const float4 xj = __ldg(sp + j);
+                const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+                rho = fa(rho, density_term(S, fsq(s)));
+            });
             if (!valid) continue;
+        } else {
             for_each_candidate(a, S, probe_of(S, xi), [&](uint32_t, float4 xj) {
                 const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
                 if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
@@ -787,19 +798,94 @@ void launch_scatter(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
 void launch_reorder(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     k_reorder<<<s.grid_p, s.tile, 0, st>>>(a);
 }
+namespace {
+// Traversal counters of one scene: [rows visited, candidates tested,
+// in-range pairs (self included)], summed with int64 atomics.
+__global__ void __launch_bounds__(256) k_traversal_stats(DevArrays a, int scene, unsigned long long* out) {
+    const SceneDev& S = a.scenes[scene];
+    unsigned long long rows = 0, cand = 0, hits = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.n; p += gridDim.x * blockDim.x) {
+        const float4 xi = a.spos[S.p_off + p];
+        const Probe q = probe_of(S, xi);
+        const int R = S.reach;
+        for (int dz = -R; dz <= R; ++dz)
+            for (int dy = -R; dy <= R; ++dy) {
+                const int z = q.c.cz + dz, y = q.c.cy + dy;
+                int xl, xh;
+                if (z < 0 || z >= S.nz || y < 0 || y >= S.ny || !row_span(S, q, y, z, &xl, &xh)) continue;
+                const uint32_t row = row_key(a.tab, S, y, z);
+                const uint32_t st = a.offsets[S.k_off + row + xl], en = a.offsets[S.k_off + row + xh + 1];
+                ++rows;
+                for (uint32_t j = st; j < en; ++j) {
+                    const float4 xj = a.spos[S.p_off + j];
+                    ++cand;
+                    hits += dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z)) <= S.smax;
+                }
+            }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        rows += __shfl_down_sync(kFull, rows, o);
+        cand += __shfl_down_sync(kFull, cand, o);
+        hits += __shfl_down_sync(kFull, hits, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, rows);
+        atomicAdd(out + 1, cand);
+        atomicAdd(out + 2, hits);
+    }
+}
+
+__global__ void k_gather_by_id(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                               const float4* __restrict__ dyn, int p_off, int n, float* __restrict__ pos3,
+                               float* __restrict__ vel3, float* __restrict__ dens, int32_t* __restrict__ sed) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float4 x = pos[p_off + p];
+    const int id = __float_as_int(x.w);
+    if (id < 0 || id >= n) return;
+    if (pos3) {
+        pos3[3 * id] = x.x;
+        pos3[3 * id + 1] = x.y;
+        pos3[3 * id + 2] = x.z;
+    }
+    if (vel3 || sed) {
+        const float4 v = vel[p_off + p];
+        if (vel3) {
+            vel3[3 * id] = v.x;
+            vel3[3 * id + 1] = v.y;
+            vel3[3 * id + 2] = v.z;
+        }
+        if (sed) sed[id] = __float_as_int(v.w);
+    }
+    if (dens) dens[id] = dyn[p_off + p].x;
+}
+}  // namespace
+
+void launch_traversal_stats(const DevArrays& a, int scene, unsigned long long* out, cudaStream_t st) {
+    k_traversal_stats<<<304, 256, 0, st>>>(a, scene, out);
+}
+
+void launch_gather_by_id(const float4* pos, const float4* vel, const float4* dyn, int p_off, int n, float* pos3,
+                         float* vel3, float* dens, int32_t* sed, cudaStream_t st) {
+    if (n > 0) k_gather_by_id<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, dyn, p_off, n, pos3, vel3, dens, sed);
+}
+
 void configure_kernels() {
     const int bytes = kListCap * kMaxTile * (int)sizeof(uint32_t);
-    cudaFuncSetAttribute(k_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_density<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.tile * sizeof(uint32_t); }
 
 void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_density<false><<<s.grid_p, s.tile, 0, st>>>(a);
+    if (s.variant & 1)
+        k_density<false, true><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+    else
+        k_density<false, false><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_density<true><<<s.grid_p, s.tile, 0, st>>>(a);
+    k_density<true, false><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     k_force<false><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);

@@ -48,6 +48,7 @@ struct LaunchShape {
     int grid_p;      // persistent grid of particle kernels
     int grid_c;      // persistent grid of the scan
     int grid_t;      // persistent grid of the terrain kernel
+    int variant;     // sph_system_config.variant bits
 };
 
 // Once per process and device: opt the list-traversal kernels into >48 KB of
@@ -66,6 +67,11 @@ void launch_tick(const DevArrays& a, int nscenes, cudaStream_t st);
 
 // Inspection and on-demand kernels.
 void launch_neighbour_counts(const DevArrays& a, const LaunchShape& s, int32_t* out_by_id, cudaStream_t st);
+// [rows visited, candidates tested, in-range pairs] of one scene's sorted state.
+void launch_traversal_stats(const DevArrays& a, int scene, unsigned long long* out, cudaStream_t st);
+// Scatter a scene's state into id order: any output may be null.
+void launch_gather_by_id(const float4* pos, const float4* vel, const float4* dyn, int p_off, int n, float* pos3,
+                         float* vel3, float* dens, int32_t* sed, cudaStream_t st);
 // Per-scene FP64 partial sums: kDiagBlocks blocks per listed scene.
 constexpr int kDiagBlocks = 32;
 constexpr int kDiagDoubles = 8;  // mass-weighted momentum xyz, kinetic, potential, (pad)

@@ -63,7 +63,7 @@ class SystemConfig(C.Structure):
     _fields_ = [
         ("device", C.c_int), ("particle_capacity", C.c_int64), ("key_capacity", C.c_int64),
         ("terrain_capacity", C.c_int64), ("max_scenes", C.c_int), ("tile", C.c_int), ("graph_steps", C.c_int),
-        ("hbm_budget", C.c_int64),
+        ("variant", C.c_int), ("hbm_budget", C.c_int64),
     ]
 
 
@@ -96,17 +96,21 @@ class ServerConfig(C.Structure):
 
 
 class TuneResult(C.Structure):
-    _fields_ = [("tile", C.c_int), ("cell_mult", C.c_float), ("ms_per_step", C.c_float), ("n_tried", C.c_int),
-                ("tiles", C.c_int * 8), ("cell_mults", C.c_float * 8), ("ms", C.c_float * 8)]
+    _fields_ = [("tile", C.c_int), ("cell_mult", C.c_float), ("variant", C.c_int), ("ms_per_step", C.c_float),
+                ("n_tried", C.c_int), ("tiles", C.c_int * 8), ("cell_mults", C.c_float * 8),
+                ("variants", C.c_int * 8), ("ms", C.c_float * 8)]
 
     def as_dict(self):
-        return {"tile": self.tile, "cell_mult": self.cell_mult, "ms_per_step": self.ms_per_step,
-                "tried": [(self.tiles[i], self.cell_mults[i], self.ms[i]) for i in range(self.n_tried)]}
+        return {"tile": self.tile, "cell_mult": self.cell_mult, "variant": self.variant,
+                "ms_per_step": self.ms_per_step,
+                "tried": [(self.tiles[i], self.cell_mults[i], self.variants[i], self.ms[i])
+                          for i in range(self.n_tried)]}
 
 
 _lib = None
 SIGNATURES = {
     "sph_system_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(TuneResult)]),
+    "sph_scene_traversal_stats": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "sph_last_error": (C.c_char_p, []),
     "sph_params_default": (None, [C.POINTER(Params)]),
     "sph_system_config_default": (None, [C.POINTER(SystemConfig)]),
@@ -444,6 +448,11 @@ class Scene:
         out = np.zeros(self.count(), np.int32)
         _ck(lib().sph_scene_neighbour_counts(self.h, self.id, _p(out)))
         return out
+
+    def traversal_stats(self) -> dict:
+        out = np.zeros(4, np.int64)
+        _ck(lib().sph_scene_traversal_stats(self.h, self.id, _p(out)))
+        return {"particles": int(out[0]), "rows": int(out[1]), "candidates": int(out[2]), "in_range": int(out[3])}
 
     def grid_dims(self):
         out = np.zeros(4, np.int32)

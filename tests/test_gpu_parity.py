@@ -134,10 +134,14 @@ def test_neighbour_counts_bit_exact(oracle_lib, golden, name, key, h):
         sc = sysm.scene(S.default_params(**prm))
         sc.set_particles(pos)
         cnt = sc.neighbour_counts()
+        stats = sc.traversal_stats()
     cnt_key = {"rec100": "cnt100", "rec1": "cnt1"}.get(key)
     if cnt_key in g:
         assert np.array_equal(cnt, g[cnt_key])
     assert np.array_equal(cnt, oracle_lib.neighbour_counts(pos, h))
+    # the trimmed traversal tests every in-range pair (self included) exactly once
+    assert stats["in_range"] == int(cnt.sum()) + len(pos)
+    assert stats["candidates"] >= stats["in_range"]
 
 
 @pytest.mark.parametrize("cell_mult", [1.0, 0.5, 1.5])
