@@ -343,7 +343,7 @@ def main():
                     choices=["plain_1m", "plain_small", "batched", "serving", "skew"])
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep --tile/--cell-mult instead of autotuning them")
-    ap.add_argument("--tile", type=int, default=512)
+    ap.add_argument("--tile", type=int, default=256)
     ap.add_argument("--cell-mult", type=float, default=0.5)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")

@@ -105,10 +105,11 @@ typedef struct sph_system_config {
     int64_t key_capacity;
     int64_t terrain_capacity;
     int max_scenes;
-    int tile;                 /* particles per work tile: 128, 256 or 512 (0 = 256) */
+    int tile;                 /* particles per work tile: 128 or 256 (0 = 256) */
     int graph_steps;          /* steps per captured CUDA graph (0 = no graphs) */
     int variant;              /* kernel variant bits, picked by the autotuner:
-                                 1 = density pass over compacted neighbour lists */
+                                 1 = density pass over compacted neighbour lists,
+                                 4 = relaxed register budget (fewer resident blocks) */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;
 
@@ -137,9 +138,10 @@ SPH_API int sph_system_memory(sph_system* s, int64_t* bytes);
 
 /* Autotuner (no counterpart in the reference).  Times `steps` steps of the
  * system's current scenes under each candidate of particles per work tile
- * (block size 256 or 512), grid cell edge (cell_mult 1 or 0.5, i.e. 27 cells
- * of h or 125 cells of h/2 around a particle) and density-pass variant
- * (direct or compacted lists), each trial starting from the same snapshot of
+ * (block size 128 or 256), grid cell edge (cell_mult 1 or 0.5, i.e. 27 cells
+ * of h or 125 cells of h/2 around a particle) and kernel variant (density
+ * pass direct or over compacted lists; high-occupancy or relaxed register
+ * budget of the neighbour kernels), each trial starting from the same snapshot of
  * every scene's state, then keeps the fastest and restores the state.  One
  * particle per thread (32 per warp) and a re-sort every step are fixed: the
  * exact neighbour sets need the current sort.  In fast mode the cell size
@@ -151,10 +153,10 @@ typedef struct sph_tune_result {
     int variant;
     float ms_per_step;
     int n_tried;
-    int tiles[8];
-    float cell_mults[8];
-    int variants[8];
-    float ms[8];
+    int tiles[16];
+    float cell_mults[16];
+    int variants[16];
+    float ms[16];
 } sph_tune_result;
 SPH_API int sph_system_autotune(sph_system* s, int steps, sph_tune_result* out);
 
@@ -251,7 +253,7 @@ typedef struct sph_server sph_server;
 
 typedef struct sph_server_config {
     int device;
-    int tile;                     /* particles per work tile (0 = 512) */
+    int tile;                     /* particles per work tile (0 = 256) */
     float cell_mult;              /* grid cell edge / h (0 = 0.5) */
     int chunk_steps;              /* steps per batched launch sequence (CUDA graph), 0 = 16 */
     int64_t hbm_budget;           /* bytes the server may hold (0 = 120 GiB) */

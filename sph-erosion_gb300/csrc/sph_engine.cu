@@ -15,8 +15,8 @@ void check_cuda(cudaError_t e, const char* what) {
 
 namespace {
 
-constexpr int kPAlign = kMaxTile;  // particle ranges start on a tile boundary for every tile size
-constexpr int64_t kTAlign = kMaxTile;
+constexpr int kPAlign = kRangeAlign;  // particle ranges start on a tile boundary for every tile size
+constexpr int64_t kTAlign = kRangeAlign;
 
 int64_t round_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
@@ -162,8 +162,7 @@ void DevBuf<T>::release() {
 // ---- System -----------------------------------------------------------------
 System::System(const sph_system_config& cfg) : cfg_(cfg) {
     if (cfg_.tile == 0) cfg_.tile = 256;
-    if (cfg_.tile != 128 && cfg_.tile != 256 && cfg_.tile != 512)
-        throw Error(SPH_ERR_INVALID, "tile must be 128, 256 or 512");
+    if (cfg_.tile != 128 && cfg_.tile != 256) throw Error(SPH_ERR_INVALID, "tile must be 128 or 256");
     if (cfg_.max_scenes <= 0) cfg_.max_scenes = 1024;
     dev_ = cfg_.device;
     SPH_CK(cudaSetDevice(dev_));
@@ -1144,9 +1143,9 @@ void System::autotune(int steps, sph_tune_result* out) {
         sdel.release();
         shgt.release();
     };
-    const int tiles[2] = {256, 512};
+    const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
-    const int variants[2] = {0, 1};
+    const int variants[4] = {0, 1, 4, 5};
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;
     float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;

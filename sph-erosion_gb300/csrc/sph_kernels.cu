@@ -122,28 +122,111 @@ __device__ __forceinline__ bool row_span(const SceneDev& S, const Probe& q, int 
     return true;
 }
 
-// Visit every candidate of the (2R+1)^2 cell rows around the particle,
-// trimmed to the h-sphere (x-adjacent cells of a row are contiguous in key
-// order).  f(j, xj) receives the scene-local sorted index and the position.
-template <class F>
-__device__ __forceinline__ void for_each_candidate(const DevArrays& a, const SceneDev& S, const Probe& q, F&& f) {
-    const int R = S.reach;
+// Cell rows of the neighbour search.  for_rows(a, S, xi, valid, fn) calls
+// fn(st, en) for each of the (2R+1)^2 rows (dz outer, dy inner, both
+// ascending) with the particle range [st, en) of the row's cells that the
+// h-sphere around xi can reach; a row it cannot reach (or any row when
+// valid is false) gives an empty range, so every lane makes the same calls.
+// The reach test is conservative (h enlarged by hcell's slack): only
+// out-of-range candidates are ever dropped and the in-range visiting order is
+// that of the full (2R+1)^3 block.
+//
+// For R = 1 and 2 (cells of h and h/2) the squared gaps of the 2R+1 cells
+// along x are computed once per particle (registers), so a row costs a few
+// adds and compares; the row loops stay rolled to keep register pressure (and
+// so occupancy) where these latency-bound kernels need it.  Other reaches
+// take the general path.
+template <int R, class Fn>
+__device__ __forceinline__ void for_rows_r(const DevArrays& a, const SceneDev& S, float4 xi, bool valid, Fn&& fn) {
+    const Probe q = probe_of(S, xi);
     const uint32_t* off = a.offsets + S.k_off;
-    const float4* sp = a.spos + S.p_off;
+    const uint32_t* tab = a.tab + S.tab_off;
+    const float H2 = S.hcell * S.hcell;
+    float gx2[2 * R + 1];
+#pragma unroll
+    for (int d = -R; d <= R; ++d) {
+        const int k = q.c.cx + d;
+        float g2 = INFINITY;
+        if (k >= 0 && k < S.nx) {
+            const float g = cell_gap(q.tx, k, S.nx);
+            g2 = g * g;
+        }
+        gx2[d + R] = g2;
+    }
+    const bool live = valid && q.finite;
+#pragma unroll 1
     for (int dz = -R; dz <= R; ++dz) {
         const int z = q.c.cz + dz;
-        if (z < 0 || z >= S.nz) continue;
+        const bool zin = live && z >= 0 && z < S.nz;
+        float gz2 = INFINITY;
+        uint32_t kz = 0;
+        if (zin) {
+            const float g = cell_gap(q.tz, z, S.nz);
+            gz2 = g * g;
+            kz = __ldg(tab + S.ny + z);
+        }
+#pragma unroll 1
         for (int dy = -R; dy <= R; ++dy) {
             const int y = q.c.cy + dy;
-            if (y < 0 || y >= S.ny) continue;
-            int xl, xh;
-            if (!row_span(S, q, y, z, &xl, &xh)) continue;
-            const uint32_t row = row_key(a.tab, S, y, z);
-            const uint32_t st = __ldg(off + row + xl);
-            const uint32_t en = __ldg(off + row + xh + 1);
-            for (uint32_t j = st; j < en; ++j) f(j, __ldg(sp + j));
+            uint32_t st = 0, en = 0;
+            if (zin && y >= 0 && y < S.ny) {
+                const float g = cell_gap(q.ty, y, S.ny);
+                const float r2 = H2 - g * g - gz2;
+                if (r2 >= 0.0f) {
+                    int lo = 0, hi = 0;  // farthest reachable cell on each side
+#pragma unroll
+                    for (int d = 1; d <= R; ++d) {
+                        if (gx2[R - d] <= r2) lo = -d;
+                        if (gx2[R + d] <= r2) hi = d;
+                    }
+                    const uint32_t row = (__ldg(tab + y) | kz) * (uint32_t)S.nx;
+                    st = __ldg(off + row + q.c.cx + lo);
+                    en = __ldg(off + row + q.c.cx + hi + 1);
+                }
+            }
+            fn(st, en);
         }
     }
+}
+
+template <class Fn>
+__device__ __forceinline__ void for_rows_any(const DevArrays& a, const SceneDev& S, float4 xi, bool valid, Fn&& fn) {
+    const Probe q = probe_of(S, xi);
+    const int R = S.reach;
+    const uint32_t* off = a.offsets + S.k_off;
+    for (int dz = -R; dz <= R; ++dz) {
+        for (int dy = -R; dy <= R; ++dy) {
+            const int z = q.c.cz + dz, y = q.c.cy + dy;
+            uint32_t st = 0, en = 0;
+            int xl, xh;
+            if (valid && z >= 0 && z < S.nz && y >= 0 && y < S.ny && row_span(S, q, y, z, &xl, &xh)) {
+                const uint32_t row = row_key(a.tab, S, y, z);
+                st = __ldg(off + row + xl);
+                en = __ldg(off + row + xh + 1);
+            }
+            fn(st, en);
+        }
+    }
+}
+
+template <class Fn>
+__device__ __forceinline__ void for_rows(const DevArrays& a, const SceneDev& S, float4 xi, bool valid, Fn&& fn) {
+    if (S.reach == 2)
+        for_rows_r<2>(a, S, xi, valid, fn);
+    else if (S.reach == 1)
+        for_rows_r<1>(a, S, xi, valid, fn);
+    else
+        for_rows_any(a, S, xi, valid, fn);
+}
+
+// Visit every candidate of the trimmed rows around xi: f(j, xj) receives the
+// scene-local sorted index and the position.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const DevArrays& a, const SceneDev& S, float4 xi, F&& f) {
+    const float4* sp = a.spos + S.p_off;
+    for_rows(a, S, xi, true, [&](uint32_t st, uint32_t en) {
+        for (uint32_t j = st; j < en; ++j) f(j, __ldg(sp + j));
+    });
 }
 
 // In-range traversal of the fast path.  Candidates are tested in a tight
@@ -163,38 +246,26 @@ constexpr int kListCap = 32;
 template <class F>
 __device__ __forceinline__ void for_each_in_range_listed(const DevArrays& a, const SceneDev& S, bool valid,
                                                          float4 xi, uint32_t* list, F&& f) {
-    const int R = S.reach;
-    const Probe pr = probe_of(S, xi);
-    const uint32_t* off = a.offsets + S.k_off;
     const float4* sp = a.spos + S.p_off;
     uint32_t* my = list + threadIdx.x;
     const int stride = blockDim.x;
     int cnt = 0;
-    for (int dz = -R; dz <= R; ++dz) {
-        for (int dy = -R; dy <= R; ++dy) {
-            const int z = pr.c.cz + dz, y = pr.c.cy + dy;
-            uint32_t st = 0, len = 0;
-            int xl, xh;
-            if (valid && z >= 0 && z < S.nz && y >= 0 && y < S.ny && row_span(S, pr, y, z, &xl, &xh)) {
-                const uint32_t row = row_key(a.tab, S, y, z);
-                st = __ldg(off + row + xl);
-                len = __ldg(off + row + xh + 1) - st;
+    for_rows(a, S, xi, valid, [&](uint32_t st, uint32_t en) {
+        const uint32_t len = en - st;
+        const uint32_t maxlen = __reduce_max_sync(kFull, len);
+        for (uint32_t t = 0; t < maxlen; ++t) {
+            if (t < len) {
+                const uint32_t j = st + t;
+                const float4 xj = __ldg(sp + j);
+                const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+                if (s <= S.smax) my[(cnt++) * stride] = j;
             }
-            const uint32_t maxlen = __reduce_max_sync(kFull, len);
-            for (uint32_t t = 0; t < maxlen; ++t) {
-                if (t < len) {
-                    const uint32_t j = st + t;
-                    const float4 xj = __ldg(sp + j);
-                    const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
-                    if (s <= S.smax) my[(cnt++) * stride] = j;
-                }
-                if (__any_sync(kFull, cnt == kListCap)) {
-                    for (int q = 0; q < cnt; ++q) f(my[q * stride]);
-                    cnt = 0;
-                }
+            if (__any_sync(kFull, cnt == kListCap)) {
+                for (int q = 0; q < cnt; ++q) f(my[q * stride]);
+                cnt = 0;
             }
         }
-    }
+    });
     for (int q = 0; q < cnt; ++q) f(my[q * stride]);
 }
 
@@ -209,8 +280,7 @@ __device__ __forceinline__ bool for_each_in_range_ordered(const DevArrays& a, co
     unsigned long long lst[kMaxNb];
     int cnt = 0;
     bool overflow = false;
-    const Probe c = probe_of(S, xi);
-    for_each_candidate(a, S, c, [&](uint32_t j, float4 xj) {
+    for_each_candidate(a, S, xi, [&](uint32_t j, float4 xj) {
         float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
         if (s <= S.smax) {
             if (cnt < kMaxNb)
@@ -538,8 +608,8 @@ __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
 // LISTED: the in-range pairs are compacted (for_each_in_range_listed) instead
 // of evaluated inside the candidate loop; which one is faster depends on the
 // neighbour density, so the autotuner picks it.
-template <bool ORDERED, bool LISTED>
-__global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
+template <bool ORDERED, bool LISTED, int MINB>
+__global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -567,7 +637,7 @@ __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
             });
             if (!valid) continue;
         } else {
-            for_each_candidate(a, S, probe_of(S, xi), [&](uint32_t, float4 xj) {
+            for_each_candidate(a, S, xi, [&](uint32_t, float4 xj) {
                 const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
                 if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
             });
@@ -579,8 +649,8 @@ __global__ void __launch_bounds__(kMaxTile) k_density(DevArrays a) {
 
 // force: passes 2 and 3 (fluid_system.h:127-178) and advance (:306-353) with
 // the terrain contact, the box collision and the erosion exchange.
-template <bool ORDERED>
-__global__ void __launch_bounds__(kMaxTile) k_force(DevArrays a) {
+template <bool ORDERED, int MINB>
+__global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -726,7 +796,7 @@ __global__ void __launch_bounds__(kMaxTile) k_neighbour_counts(DevArrays a, int3
         const float4 xi = a.spos[p];
         const int pl = p - S.p_off;
         int cnt = 0;
-        for_each_candidate(a, S, probe_of(S, xi), [&](uint32_t j, float4 xj) {
+        for_each_candidate(a, S, xi, [&](uint32_t j, float4 xj) {
             float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
             if (s <= S.smax && (int)j != pl) ++cnt;
         });
@@ -872,26 +942,41 @@ void launch_gather_by_id(const float4* pos, const float4* vel, const float4* dyn
 
 void configure_kernels() {
     const int bytes = kListCap * kMaxTile * (int)sizeof(uint32_t);
-    cudaFuncSetAttribute(k_density<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_density<false, true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_density<false, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.tile * sizeof(uint32_t); }
 
+// Variant bit 2 relaxes the register budget of the two neighbour kernels
+// (fewer resident blocks, no spills) against the default high occupancy.
 void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    if (s.variant & 1)
-        k_density<false, true><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
-    else
-        k_density<false, false><<<s.grid_p, s.tile, 0, st>>>(a);
+    const bool relaxed = (s.variant & 4) != 0;
+    if (s.variant & 1) {
+        if (relaxed)
+            k_density<false, true, 4><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+        else
+            k_density<false, true, 8><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+    } else {
+        if (relaxed)
+            k_density<false, false, 4><<<s.grid_p, s.tile, 0, st>>>(a);
+        else
+            k_density<false, false, 8><<<s.grid_p, s.tile, 0, st>>>(a);
+    }
 }
 void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_density<true, false><<<s.grid_p, s.tile, 0, st>>>(a);
+    k_density<true, false, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_force<false><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+    if (s.variant & 4)
+        k_force<false, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+    else
+        k_force<false, 4><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
 }
 void launch_force_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_force<true><<<s.grid_p, s.tile, 0, st>>>(a);
+    k_force<true, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_terrain(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     k_terrain<<<s.grid_t, s.tile, 0, st>>>(a);

@@ -118,7 +118,7 @@ class Server {
         sph_system_config s;
         sph_system_config_default(&s);
         s.device = c.device;
-        s.tile = c.tile > 0 ? c.tile : 512;
+        s.tile = c.tile > 0 ? c.tile : 256;
         s.graph_steps = c.chunk_steps > 0 ? c.chunk_steps : 16;
         s.hbm_budget = c.hbm_budget > 0 ? c.hbm_budget : ((int64_t)120 << 30);
         s.max_scenes = c.max_scenes > 0 ? c.max_scenes : 4096;
@@ -271,7 +271,7 @@ SPH_API int sph_scene_from_request(sph_system* s, const sph_params* base, const 
 SPH_API void sph_server_config_default(sph_server_config* c) {
     if (!c) return;
     std::memset(c, 0, sizeof *c);
-    c->tile = 512;
+    c->tile = 256;
     c->cell_mult = 0.5f;
     c->chunk_steps = 16;
     c->hbm_budget = (int64_t)120 << 30;

@@ -10,7 +10,8 @@ namespace sph {
 constexpr int kChunkBits = 12;
 constexpr int kChunk = 1 << kChunkBits;
 constexpr int kScanThreads = 256;           // 16 keys per thread
-constexpr int kMaxTile = 512;
+constexpr int kMaxTile = 256;    // particles per work tile: 128 or 256
+constexpr int kRangeAlign = 512; // particle and terrain ranges start on this boundary
 
 enum SceneFlags : int {
     kFlagTerrain = 1,

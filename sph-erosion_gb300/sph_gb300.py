@@ -97,8 +97,8 @@ class ServerConfig(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("tile", C.c_int), ("cell_mult", C.c_float), ("variant", C.c_int), ("ms_per_step", C.c_float),
-                ("n_tried", C.c_int), ("tiles", C.c_int * 8), ("cell_mults", C.c_float * 8),
-                ("variants", C.c_int * 8), ("ms", C.c_float * 8)]
+                ("n_tried", C.c_int), ("tiles", C.c_int * 16), ("cell_mults", C.c_float * 16),
+                ("variants", C.c_int * 16), ("ms", C.c_float * 16)]
 
     def as_dict(self):
         return {"tile": self.tile, "cell_mult": self.cell_mult, "variant": self.variant,
@@ -169,7 +169,7 @@ def requests_array(reqs):
 class Server:
     """Continuous-batching request server (include/sph_erosion.h)."""
 
-    def __init__(self, base: Params = None, tile=512, cell_mult=0.5, chunk_steps=16, hbm_budget=0,
+    def __init__(self, base: Params = None, tile=256, cell_mult=0.5, chunk_steps=16, hbm_budget=0,
                  max_active_particles=0, max_scenes=0, device=0):
         cfg = ServerConfig()
         lib().sph_server_config_default(C.byref(cfg))

@@ -23,7 +23,7 @@ def _state(scene):
     return st["pos"], st["vel"], st["sed"]
 
 
-def _alone(req, steps, tile=512, cell_mult=0.5):
+def _alone(req, steps, tile=256, cell_mult=0.5):
     with S.System(tile=tile) as sysm:
         sc = sysm.scene_from_request(W.base_params(cell_mult), req)
         sysm.step(steps)
@@ -46,7 +46,7 @@ def test_recipe_scene_shape():
 
 def test_batched_equals_alone_bitwise():
     steps = 20
-    with S.System(tile=512) as sysm:
+    with S.System(tile=128) as sysm:
         scenes = [sysm.scene_from_request(W.base_params(), r) for r in SMALL]
         sysm.step(steps)
         mixed = [(_state(sc), sc.diag()) for sc in scenes]
@@ -110,7 +110,7 @@ def test_autotune_restores_state_and_applies_choice():
         sysm.step(5)
         before = [_state(sc) for sc in scenes]
         tuned = sysm.autotune(4)
-        assert len(tuned["tried"]) == 8 and tuned["tile"] in (256, 512) and tuned["variant"] in (0, 1)
+        assert len(tuned["tried"]) == 16 and tuned["tile"] in (128, 256) and tuned["variant"] in (0, 1, 4, 5)
         assert tuned["ms_per_step"] == min(t[3] for t in tuned["tried"])
         for sc, st in zip(scenes, before):
             for a, b in zip(_state(sc), st):

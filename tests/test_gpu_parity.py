@@ -201,10 +201,10 @@ def test_graph_eager_and_tile_paths_identical(golden):
     a = run(C1, g["pos0"], 40, graph_steps=16)[40][0]
     b = run(C1, g["pos0"], 40, graph_steps=0)[40][0]
     c = run(C1, g["pos0"], 40, graph_steps=16, tile=128)[40][0]
-    d = run(C1, g["pos0"], 40, graph_steps=16, tile=512)[40][0]
+    d = run(C1, g["pos0"], 40, graph_steps=16, tile=256)[40][0]
     assert np.array_equal(a, b) and np.array_equal(a, c) and np.array_equal(a, d)
     e = run(C1, g["pos0"], 40, flags=ORDERED)[40][0]
-    f = run(C1, g["pos0"], 40, flags=ORDERED, tile=512, cell_mult=0.5)[40][0]
+    f = run(C1, g["pos0"], 40, flags=ORDERED, tile=128, cell_mult=0.5)[40][0]
     assert np.array_equal(e, f)
     h = run(C1, g["pos0"], 40, cell_mult=0.5)[40][0]
     assert max(field_errors(h, a).values()) <= RTOL
