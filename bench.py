@@ -267,68 +267,121 @@ def run_ours(args, spec, config):
 C_PARAMS_BYTES = 4 * 24
 
 
+def _init_ranks():
+    """Rank setup of the batched and served modes: scenes shard across ranks
+    (no data-path collective), gloo carries the final metric reduction."""
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    return ws, rank, local
+
+
+def _gather(value, ws):
+    if ws == 1:
+        return [value]
+    import torch.distributed as dist
+
+    out = [None] * ws
+    dist.all_gather_object(out, value)
+    return out
+
+
 def run_batched(args, config):
     """Batched form vs plain form on the same seeded scenes: all scenes in one
     system (one launch per stage for all of them, 16-step CUDA graphs) against
-    each scene alone in its own system, timed scene after scene."""
-    import torch
-
+    each scene alone in its own system, timed scene after scene.  With N ranks
+    each rank runs its cost-balanced share of the scenes."""
+    import shard
     import sph_gb300 as S
     import workloads as W
 
-    torch.cuda.set_device(0)
-    reqs = W.batched_requests(args.scenes)
+    ws, rank, local = _init_ranks()
+    all_reqs = W.batched_requests(args.scenes)
+    reqs = shard.shard_requests(all_reqs, ws, rank)
     total = sum(r["particles"] for r in reqs)
+    total_all = sum(r["particles"] for r in all_reqs)
     base = W.base_params(args.cell_mult)
     sysm = S.System(particle_capacity=total + 512 * len(reqs), key_capacity=1 << 24, terrain_capacity=1 << 24,
-                    tile=args.tile, graph_steps=16)
+                    tile=args.tile, graph_steps=16, device=local)
     for r in reqs:
         sysm.scene_from_request(base, r)
     sysm.step(args.warmup)
     sysm.sync()
+    tuned = sysm.autotune(4) if args.autotune else None
     with Clocks() as clk:
-        ms = sysm.time_steps(args.steps)
-    batched = total * args.steps / (ms * 1e-3)
+        ms = barrier_max(sysm.time_steps(args.steps), ws)
+    batched = total_all * args.steps / (ms * 1e-3)
     sysm.close()
-    # plain form: one system per scene, same steps
+    # plain form: one system per scene, same steps, same tuned tile and cell
+    tile = tuned["tile"] if tuned else args.tile
+    cm = tuned["cell_mult"] if tuned else args.cell_mult
     plain_ms = 0.0
     for r in reqs:
-        with S.System(particle_capacity=r["particles"], tile=args.tile, graph_steps=16) as one:
-            one.scene_from_request(base, r)
+        with S.System(particle_capacity=r["particles"], tile=tile, graph_steps=16, device=local) as one:
+            one.scene_from_request(W.base_params(cm), r)
             one.step(args.warmup)
             one.sync()
             plain_ms += one.time_steps(args.steps)
-    plain = total * args.steps / (plain_ms * 1e-3)
-    line = {"metric": METRIC, "value": batched, "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+    plain_ms = barrier_max(plain_ms, ws)
+    plain = total_all * args.steps / (plain_ms * 1e-3)
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": batched, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-            "config": dict(config, workload="batched", scenes=len(reqs), particles=total,
-                           l2="inputs larger than L2 (%.0f MB of particle state)" % (total * 100 / 1e6)),
+            "config": dict(config, workload="batched", scenes=len(all_reqs), particles=total_all,
+                           parallelism=f"scenes sharded over {ws} rank(s)",
+                           l2="inputs larger than L2 (%.0f MB of particle state)" % (total_all * 100 / 1e6)),
             "plain_value": plain, "batched_over_plain": batched / plain, "plain_ms_per_step": plain_ms / args.steps,
-            "clocks": clk.summary()}
+            "tuned": tuned, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
 
 def run_serving(args, config):
     """Served form: a Poisson request trace replayed in real time through the
-    continuous-batching server."""
+    continuous-batching server.  With N ranks each rank serves its
+    cost-balanced share of the trace; throughput is the job's particle-steps
+    over the slowest rank's wall time, latencies are pooled."""
+    import numpy as np
+
+    import shard
     import sph_gb300 as S
     import workloads as W
 
-    trace = W.serving_trace(args.requests, rate=args.rate)
+    ws, rank, local = _init_ranks()
+    full = W.serving_trace(args.requests, rate=args.rate)
+    trace = shard.shard_requests(full, ws, rank)
     with Clocks() as clk, S.Server(W.base_params(args.cell_mult), tile=args.tile, chunk_steps=16,
-                                    hbm_budget=120 << 30) as srv:
+                                    hbm_budget=120 << 30, device=local) as srv:
         res, st = srv.run_trace(trace)
+    lat = [r.done_s - r.arrival_s for r in res]
     bad = sum(1 for r in res if r.total_units != 0 or r.nan_particles != 0)
-    line = {"metric": METRIC, "value": st["throughput"], "unit": "particle-steps/s", "n_gpus": 1,
-            "steps": int(sum(r["steps"] for r in trace)), "warmup": 0, "ms_per_step": None,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+    parts = _gather(dict(lat=lat, bad=bad, ps=st["particle_steps"], wall=st["wall_s"], peak=st["peak_active"],
+                         peak_p=st["peak_particles"], peak_b=st["peak_bytes"], chunks=st["chunks"]), ws)
+    if rank != 0:
+        return
+    lat = np.sort(np.concatenate([np.asarray(q["lat"]) for q in parts]))
+
+    def pct(q):
+        return float(lat[min(len(lat) - 1, max(0, int(np.ceil(q * len(lat))) - 1))])
+
+    wall = max(q["wall"] for q in parts)
+    ps = sum(q["ps"] for q in parts)
+    line = {"metric": METRIC, "value": ps / wall, "unit": "particle-steps/s", "n_gpus": ws,
+            "steps": int(sum(r["steps"] for r in full)), "warmup": 0, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Poisson request trace)",
-            "config": dict(config, workload="serving", requests=len(trace), rate_per_s=args.rate,
-                           hbm_budget_gb=120),
-            "p50_latency_s": st["p50_s"], "p99_latency_s": st["p99_s"], "max_latency_s": st["max_s"],
-            "wall_s": st["wall_s"], "peak_active": st["peak_active"], "peak_particles": st["peak_particles"],
-            "peak_bytes": st["peak_bytes"], "chunks": st["chunks"], "mass_violations": bad,
+            "config": dict(config, workload="serving", requests=len(full), rate_per_s=args.rate,
+                           hbm_budget_gb=120, parallelism=f"requests sharded over {ws} rank(s)"),
+            "p50_latency_s": pct(0.50), "p99_latency_s": pct(0.99), "max_latency_s": float(lat[-1]),
+            "wall_s": wall, "peak_active": max(q["peak"] for q in parts),
+            "peak_particles": max(q["peak_p"] for q in parts), "peak_bytes": max(q["peak_b"] for q in parts),
+            "chunks": sum(q["chunks"] for q in parts), "mass_violations": sum(q["bad"] for q in parts),
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 

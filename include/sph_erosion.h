@@ -200,6 +200,11 @@ SPH_API int sph_scene_set_terrain(sph_system* s, int scene, int w, int d, const 
  * repository's own generator). */
 SPH_API int sph_scene_gen_terrain(sph_system* s, int scene, uint64_t seed, int octaves, float amplitude,
                           float lacunarity, float gain, int kind);
+/* LoadHeightfield (grid.h:98-102): the reference's 512 x 512 8-bit map,
+ * x-major (map[512 * x + z]), becomes the scene's 512 x 512 FP32 terrain at
+ * metres_per_level per grey level; deltas reset to zero. */
+SPH_API int sph_scene_load_heightfield_u8(sph_system* s, int scene, const unsigned char* map512,
+                                          float metres_per_level);
 /* Current heights (base + delta) and the int64 deltas (either may be NULL). */
 SPH_API int sph_scene_get_terrain(sph_system* s, int scene, float* heights, int64_t* delta);
 SPH_API int sph_scene_terrain_dims(sph_system* s, int scene, int* w, int* d);
@@ -214,6 +219,15 @@ SPH_API int sph_terrain_mesh_u8(const unsigned char* map512, int dimx, int dimy,
  * units: tw * td vertices (x, y, z, normal), z-major, and
  * 6 (tw - 1)(td - 1) indices.  The front end's per-frame terrain redraw. */
 SPH_API int sph_scene_terrain_mesh(sph_system* s, int scene, float* verts, unsigned* indices);
+
+/* ---- checkpoint / restore (no counterpart in the reference) ---------------
+ * A scene's whole state in one little-endian binary file: "SPHE", version,
+ * the sph_params block, counts, the particle records in device order
+ * (position + id, velocity + sediment), NeighbId, step budget, terrain base
+ * heights and int64 deltas.  Restoring into a scene (created with any
+ * parameters; they are replaced) continues bit for bit like the original. */
+SPH_API int sph_scene_save(sph_system* s, int scene, const char* path);
+SPH_API int sph_scene_load(sph_system* s, int scene, const char* path);
 
 /* ---- inspection for parity checks ---------------------------------------- */
 /* Cell key of each particle and the stable sorted order (ids), as the next

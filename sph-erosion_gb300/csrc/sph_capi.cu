@@ -128,6 +128,18 @@ int sph_system_profile_stages(sph_system* s, int nsteps, float* ms) {
     });
 }
 
+int sph_scene_save(sph_system* s, int scene, const char* path) {
+    return guard([&] { sys(s).save(scene, path); });
+}
+
+int sph_scene_load(sph_system* s, int scene, const char* path) {
+    return guard([&] { sys(s).load(scene, path); });
+}
+
+int sph_scene_load_heightfield_u8(sph_system* s, int scene, const unsigned char* map512, float metres_per_level) {
+    return guard([&] { sys(s).load_heightfield_u8(scene, map512, metres_per_level); });
+}
+
 int sph_scene_traversal_stats(sph_system* s, int scene, int64_t* out4) {
     return guard([&] {
         need(out4, "out4");

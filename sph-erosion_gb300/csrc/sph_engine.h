@@ -91,6 +91,9 @@ class System {
     void debug_sort(int id, uint32_t* keys_by_id, int32_t* sorted_ids);
     void neighbour_counts(int id, int32_t* out);
     void traversal_stats(int id, int64_t* out4);
+    void save(int id, const char* path);
+    void load(int id, const char* path);
+    void load_heightfield_u8(int id, const unsigned char* map512, float metres_per_level);
     void grid_dims(int id, int* dims4) const;
 
     void step(int nsteps);

@@ -111,6 +111,9 @@ _lib = None
 SIGNATURES = {
     "sph_system_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(TuneResult)]),
     "sph_scene_traversal_stats": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "sph_scene_save": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
+    "sph_scene_load": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
+    "sph_scene_load_heightfield_u8": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_float]),
     "sph_last_error": (C.c_char_p, []),
     "sph_params_default": (None, [C.POINTER(Params)]),
     "sph_system_config_default": (None, [C.POINTER(SystemConfig)]),
@@ -448,6 +451,18 @@ class Scene:
         out = np.zeros(self.count(), np.int32)
         _ck(lib().sph_scene_neighbour_counts(self.h, self.id, _p(out)))
         return out
+
+    def save(self, path):
+        _ck(lib().sph_scene_save(self.h, self.id, str(path).encode()))
+
+    def load(self, path):
+        _ck(lib().sph_scene_load(self.h, self.id, str(path).encode()))
+
+    def load_heightfield_u8(self, map512, metres_per_level):
+        m = np.ascontiguousarray(map512, np.uint8).ravel()
+        if m.size != 512 * 512:
+            raise ValueError("the heightfield is 512 x 512 bytes")
+        _ck(lib().sph_scene_load_heightfield_u8(self.h, self.id, _p(m), float(metres_per_level)))
 
     def traversal_stats(self) -> dict:
         out = np.zeros(4, np.int64)
