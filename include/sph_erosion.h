@@ -58,7 +58,7 @@ typedef struct sph_params {
     float smoothing_radius; /* h */
     float box_center[3];    /* the reference box is centred at 0 ... */
     float box_half[3];      /* ... with half extent len on every axis */
-    float cell_mult;        /* uniform-grid cell edge / h, >= 0.5 (default 1) */
+    float cell_mult;        /* uniform-grid cell edge / h, >= 0.25 (default 1) */
     int erosion;            /* 1 = exchange sediment with the terrain */
     float k_capacity;       /* carried volume fraction per m/s of speed */
     float k_pickup;         /* 1/s */
@@ -219,6 +219,19 @@ SPH_API int sph_terrain_mesh_u8(const unsigned char* map512, int dimx, int dimy,
  * units: tw * td vertices (x, y, z, normal), z-major, and
  * 6 (tw - 1)(td - 1) indices.  The front end's per-frame terrain redraw. */
 SPH_API int sph_scene_terrain_mesh(sph_system* s, int scene, float* verts, unsigned* indices);
+
+/* Grid::collision (Erosion/grid.h:462-805) for n queries at once: the
+ * contact of a particle moving from cur to next with velocity vel against
+ * the two triangles of each cell of the 8-bit 512 x 512 height map
+ * (map[512 * x + z], cell units), including the reference's adjacency walk
+ * (findAdjacentCell, grid.h:210-269) and corner cases (grid.h:320-440).
+ * Per query: hit 1/0, and on a hit the contact point and normal (zeros
+ * otherwise), equal bit for bit to the reference's.  dimx/dimz are the
+ * Grid's m_DimX/m_DimZ (2..512).  The reference compiles this routine but
+ * never calls it (fluid_system.h:335-340).  Host arrays, 3 floats per query. */
+SPH_API int sph_grid_collision_u8(const unsigned char* map512, int dimx, int dimz, int n, const float* cur3,
+                                  const float* next3, const float* vel3, float* contact3, float* normal3,
+                                  int32_t* hit);
 
 /* ---- checkpoint / restore (no counterpart in the reference) ---------------
  * A scene's whole state in one little-endian binary file: "SPHE", version,

@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsph_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["sph_kernels.cu", "sph_engine.cu", "sph_capi.cu", "sph_terrain.cpp", "sph_serve.cu", "sph_static.cu", "sph_recipe.cpp", "sph_mesh.cu",
-           "sph_state.cu"]
+           "sph_state.cu", "sph_gridcol.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ffp-contract=off keeps host-side FP32 constants (kernel normalisations,
 # terrain geometry) rounded exactly like the reference and the oracle on both

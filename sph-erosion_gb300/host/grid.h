@@ -4,10 +4,11 @@
 // (sph_terrain_mesh_u8) with the reference's arithmetic, bit for bit.
 //
 // The voxel array and the 512 x 512 8-bit heightfield stay on the host, as
-// in the reference (the front end reads them for drawing).  collision()
-// mirrors the reference's call site, which is disabled
-// (Erosion/fluid_system.h:335-340): the step's terrain contact is the
-// scene's FP32 heightfield (sph_scene_set_terrain), not this integer grid.
+// in the reference (the front end reads them for drawing).  collision() is
+// the reference's triangle contact on this integer grid
+// (sph_grid_collision_u8); the reference's step does not call it
+// (Erosion/fluid_system.h:335-340), and the step's terrain contact is the
+// scene's FP32 heightfield (sph_scene_set_terrain).
 #pragma once
 #include <cstring>
 #include <stdexcept>
@@ -65,12 +66,22 @@ class Grid {
                                                     VoxelType::VOXEL_MAT);
     }
 
-    // The reference's heightfield ray contact is not on the step's path (its
-    // call is commented out at fluid_system.h:335-340); contact with the
-    // terrain happens inside the step against the scene's heightfield.
-    bool collision(const sph_shim::vec3&, const sph_shim::vec3&, const sph_shim::vec3&, sph_shim::vec3&,
-                   sph_shim::vec3&) {
-        return false;
+    // The reference's triangle contact against this grid (grid.h:462-805),
+    // run on the GPU with the reference's arithmetic.  Its only call site is
+    // commented out (fluid_system.h:335-340); the step's own terrain contact
+    // is against the scene's heightfield.  As in the reference, contactP and
+    // norm are written only on a hit.
+    bool collision(const sph_shim::vec3& posCurr, const sph_shim::vec3& posNext, const sph_shim::vec3& velNext,
+                   sph_shim::vec3& contactP, sph_shim::vec3& norm) {
+        int32_t hit = 0;
+        sph_shim::vec3 cp, nr;
+        check(sph_grid_collision_u8(m_map.data(), m_DimX, m_DimZ, 1, &posCurr.x, &posNext.x, &velNext.x, &cp.x,
+                                    &nr.x, &hit));
+        if (hit) {
+            contactP = cp;
+            norm = nr;
+        }
+        return hit != 0;
     }
 
     std::vector<unsigned int> GetIndices() { return indices; }

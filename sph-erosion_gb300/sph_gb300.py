@@ -153,6 +153,8 @@ SIGNATURES = {
     "sph_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "sph_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sph_server_run_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(ServerStats)]),
+    "sph_grid_collision_u8": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -247,6 +249,27 @@ def _ck(rc: int):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def grid_collision(hmap, dims, cur, nxt, vel):
+    """Grid::collision (Erosion/grid.h:462-805) for a batch of queries on the
+    GPU.  hmap: 512 x 512 uint8 map indexed [x, z]; dims: (m_DimX, m_DimZ) or
+    the Grid's (x, y, z) dims; cur/nxt/vel: (n, 3) float32.  Returns
+    (hit bool[n], contact (n, 3), normal (n, 3))."""
+    m = np.ascontiguousarray(hmap, np.uint8)
+    if m.size != 512 * 512:
+        raise ValueError("the height map is 512 x 512")
+    dx, dz = (dims[0], dims[-1])
+    cur, nxt, vel = (np.ascontiguousarray(a, np.float32).reshape(-1, 3) for a in (cur, nxt, vel))
+    n = cur.shape[0]
+    if nxt.shape[0] != n or vel.shape[0] != n:
+        raise ValueError("cur, nxt and vel need the same number of queries")
+    cp = np.zeros((n, 3), np.float32)
+    nr = np.zeros((n, 3), np.float32)
+    hit = np.zeros(n, np.int32)
+    _ck(lib().sph_grid_collision_u8(_p(m), int(dx), int(dz), n, _p(cur), _p(nxt), _p(vel), _p(cp), _p(nr),
+                                    _p(hit)))
+    return hit.astype(bool), cp, nr
 
 
 def default_params(**overrides) -> Params:

@@ -59,6 +59,45 @@ def fp64_fixture():
     save("fp64_c1_16384.npz", state100=out["rec"][:, 0:11].astype(np.float32))
 
 
+def collision_fixture():
+    """Grid::collision (grid.h:462-805) on seeded queries over a seeded 8-bit
+    heightfield: particles above the surface moving through it, in cells that
+    keep every lookup of the routine inside the map."""
+    import ctypes as C
+
+    rng = np.random.default_rng(17)
+    hm = np.clip(O.fbm(17, 512, 512, 4, 60.0) + 40.0 + rng.uniform(0, 3, (512, 512)), 0, 255).astype(np.uint8)
+    dims = (100, 256, 100)
+    L = O.Reference().L
+    g = L.ref_grid_new(*dims)
+    L.ref_grid_load(g, np.ascontiguousarray(hm.ravel()))
+    nq = 6000
+    cur = np.zeros((nq, 3), np.float32)
+    nxt = np.zeros((nq, 3), np.float32)
+    vel = np.zeros((nq, 3), np.float32)
+    for q in range(nq):
+        x, z = rng.uniform(3.0, 95.0, 2)
+        h = float(hm.ravel()[int(x) * 512 + int(z)])
+        cur[q] = (x, h + rng.uniform(0.05, 3.0), z)
+        step = np.array([rng.uniform(-1.2, 1.2), -rng.uniform(0.1, 5.0), rng.uniform(-1.2, 1.2)])
+        if q % 5 == 0:
+            step[1] = rng.uniform(-0.5, 0.5)  # grazing motion
+        nxt[q] = cur[q] + step
+        vel[q] = step / 0.01
+    cp = np.zeros((nq, 3), np.float32)
+    nr = np.zeros((nq, 3), np.float32)
+    hit = np.zeros(nq, np.int32)
+    for q in range(nq):
+        a, b = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        hit[q] = L.ref_grid_collision(g, np.ascontiguousarray(cur[q]), np.ascontiguousarray(nxt[q]),
+                                      np.ascontiguousarray(vel[q]), a, b)
+        cp[q], nr[q] = a, b
+    L.ref_grid_free(g)
+    print("collision hits:", int(hit.sum()), "of", nq)
+    save("ref_collision.npz", hmap=hm, dims=np.array(dims, np.int32), cur=cur, next=nxt, vel=vel, contact=cp,
+         normal=nr, hit=hit)
+
+
 def main(ref_root):
     assert O.build_ref(ref_root), "reference harness did not build"
 
@@ -134,6 +173,11 @@ def main(ref_root):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if "--collision-only" in sys.argv:
+        O.build_ref(args[0] if args else "/root/reference")
+        collision_fixture()
+        sys.exit(0)
     if "--fp64-only" not in sys.argv:
         main(args[0] if args else "/root/reference")
+        collision_fixture()
     fp64_fixture()

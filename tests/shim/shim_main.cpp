@@ -5,8 +5,11 @@
 //   same after step 10
 //   int32 surface floats, floats; int32 index count, uint32 indices  (Grid::UpdateGrid)
 //   int32 count after Reset() + AddParticles(125)
+//   with a collision map and queries: int32 n, then per query int32 hit and
+//   6 floats contact + normal (Grid::collision on a Grid(dx, 256, dz))
 //
-// usage: shim_main out.bin heightmap512.bin [ordered]
+// usage: shim_main out.bin heightmap512.bin ordered|fast [collision_map512.bin queries.bin]
+//   queries.bin: int32 dx, int32 dz, int32 n, n * 9 floats (cur, next, vel)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -75,6 +78,31 @@ int main(int argc, char** argv) {
     fluidsph.Run(grid);
     int count = (int)(fluidsph.GetPositions().size() / 3);
     std::fwrite(&count, 4, 1, f);
+
+    if (argc > 5) {
+        std::vector<unsigned char> cmap(512 * 512);
+        FILE* cm = std::fopen(argv[4], "rb");
+        if (!cm || std::fread(cmap.data(), 1, cmap.size(), cm) != cmap.size()) return 5;
+        std::fclose(cm);
+        FILE* qf = std::fopen(argv[5], "rb");
+        int hdr[3];
+        if (!qf || std::fread(hdr, 4, 3, qf) != 3) return 6;
+        std::vector<float> q((size_t)hdr[2] * 9);
+        if (std::fread(q.data(), 4, q.size(), qf) != q.size()) return 7;
+        std::fclose(qf);
+        Grid cg(hdr[0], 256, hdr[1]);
+        cg.LoadHeightfield(cmap.data());
+        std::fwrite(&hdr[2], 4, 1, f);
+        for (int i = 0; i < hdr[2]; i++) {
+            const float* r = &q[(size_t)9 * i];
+            sph_shim::vec3 cp(0.0f), nr(0.0f);
+            const int32_t hit = cg.collision(sph_shim::vec3(r[0], r[1], r[2]), sph_shim::vec3(r[3], r[4], r[5]),
+                                             sph_shim::vec3(r[6], r[7], r[8]), cp, nr) ? 1 : 0;
+            const float o[6] = {cp.x, cp.y, cp.z, nr.x, nr.y, nr.z};
+            std::fwrite(&hit, 4, 1, f);
+            std::fwrite(o, 4, 6, f);
+        }
+    }
     std::fclose(f);
     return 0;
 }

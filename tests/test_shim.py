@@ -55,6 +55,11 @@ def _read(path):
     ni = int(take(np.int32, 1)[0])
     out["indices"] = take(np.uint32, ni).copy()
     out["count"] = int(take(np.int32, 1)[0])
+    if off < len(b):
+        nq = int(take(np.int32, 1)[0])
+        raw = take(np.uint8, nq * 28).reshape(nq, 28)
+        out["hit"] = raw[:, :4].copy().view(np.int32).ravel()
+        out["contact_normal"] = raw[:, 4:].copy().view(np.float32).reshape(nq, 6)
     return out
 
 
@@ -67,7 +72,16 @@ def test_shim_front_end_session_matches_reference(tmp_path, golden, ordered):
     hm = tmp_path / "hm.bin"
     hm.write_bytes(np.ascontiguousarray(m["hmap"], np.uint8).tobytes())
     out = tmp_path / "out.bin"
-    args = [exe, str(out), str(hm)] + (["ordered"] if ordered else [])
+    # Grid::collision through the drop-in, one call per query, on a slice of
+    # the reference's collision vectors
+    c = golden("ref_collision.npz")
+    cm = tmp_path / "cm.bin"
+    cm.write_bytes(np.ascontiguousarray(c["hmap"], np.uint8).tobytes())
+    nq = 600
+    q = np.concatenate([c["cur"][:nq], c["next"][:nq], c["vel"][:nq]], axis=1).astype(np.float32)
+    qf = tmp_path / "q.bin"
+    qf.write_bytes(np.array([c["dims"][0], c["dims"][2], nq], np.int32).tobytes() + q.tobytes())
+    args = [exe, str(out), str(hm), "ordered" if ordered else "fast", str(cm), str(qf)]
     subprocess.run(args, check=True, timeout=120)
     r = _read(str(out))
     rec1, nb1 = r["s1"]
@@ -80,3 +94,6 @@ def test_shim_front_end_session_matches_reference(tmp_path, golden, ordered):
     assert np.array_equal(r["surface"], m["surface"])
     assert np.array_equal(r["indices"], m["indices"])
     assert r["count"] == 1000 + 125
+    assert np.array_equal(r["hit"], c["hit"][:nq])
+    want = np.concatenate([c["contact"][:nq], c["normal"][:nq]], axis=1)
+    assert np.array_equal(r["contact_normal"].view(np.uint32), want.view(np.uint32))
