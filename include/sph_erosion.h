@@ -109,7 +109,11 @@ typedef struct sph_system_config {
     int graph_steps;          /* steps per captured CUDA graph (0 = no graphs) */
     int variant;              /* kernel variant bits, picked by the autotuner:
                                  1 = density pass over compacted neighbour lists,
-                                 4 = relaxed register budget (fewer resident blocks) */
+                                 4 = relaxed register budget (fewer resident blocks),
+                                 8 = the density pass writes each particle's in-range
+                                     neighbours (64 slots, 260 B per particle) and the
+                                     force pass reads them instead of re-testing the
+                                     cells; ignored when the HBM budget has no room */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;
 
@@ -140,8 +144,9 @@ SPH_API int sph_system_memory(sph_system* s, int64_t* bytes);
  * system's current scenes under each candidate of particles per work tile
  * (block size 128 or 256), grid cell edge (cell_mult 1 or 0.5, i.e. 27 cells
  * of h or 125 cells of h/2 around a particle) and kernel variant (density
- * pass direct or over compacted lists; high-occupancy or relaxed register
- * budget of the neighbour kernels), each trial starting from the same snapshot of
+ * pass direct or over compacted lists; neighbour lists handed from the
+ * density to the force pass; high-occupancy or relaxed register budget of
+ * the neighbour kernels), each trial starting from the same snapshot of
  * every scene's state, then keeps the fastest and restores the state.  One
  * particle per thread (32 per warp) and a re-sort every step are fixed: the
  * exact neighbour sets need the current sort.  In fast mode the cell size
@@ -153,10 +158,10 @@ typedef struct sph_tune_result {
     int variant;
     float ms_per_step;
     int n_tried;
-    int tiles[16];
-    float cell_mults[16];
-    int variants[16];
-    float ms[16];
+    int tiles[32];
+    float cell_mults[32];
+    int variants[32];
+    float ms[32];
 } sph_tune_result;
 SPH_API int sph_system_autotune(sph_system* s, int steps, sph_tune_result* out);
 

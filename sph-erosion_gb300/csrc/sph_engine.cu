@@ -197,6 +197,7 @@ System::~System() {
     for (auto* b : f4) b->release();
     key_.release(); slot_.release(); perm_.release();
     nbid_.release(); snbid_.release(); rec_.release();
+    nlist_.release(); ncnt_.release();
     counts_.release(); offsets_.release(); chunk_.release(); tab_.release();
     tbase_.release(); theight_.release(); tdelta_.release();
     dscenes_.release(); steps_.release(); ptiles_.release(); ctiles_.release(); ttiles_.release();
@@ -218,6 +219,7 @@ int64_t System::memory_bytes() const {
     int64_t b = 0;
     b += pos_.bytes() + vel_.bytes() + spos_.bytes() + svel_.bytes() + dyn_.bytes();
     b += key_.bytes() + slot_.bytes() + perm_.bytes() + nbid_.bytes() + snbid_.bytes() + rec_.bytes();
+    b += nlist_.bytes() + ncnt_.bytes();
     b += counts_.bytes() + offsets_.bytes() + chunk_.bytes() + tab_.bytes();
     b += tbase_.bytes() + theight_.bytes() + tdelta_.bytes();
     b += dscenes_.bytes() + steps_.bytes() + ptiles_.bytes() + ctiles_.bytes() + ttiles_.bytes();
@@ -262,6 +264,7 @@ void System::grow_particles(int64_t cap) {
     snbid_.resize(cap, true, st_);
     if (rec_.n) rec_.resize(cap * kRecFloats, true, st_);
     pa_.grow(cap);
+    work_dirty_ = true;  // the neighbour lists follow the arena's size
     drop_graph();
 }
 void System::grow_keys(int64_t cap) {
@@ -844,7 +847,31 @@ void System::rebuild_work() {
     n_ctiles_ = counts[1];
     n_ttiles_ = counts[2];
     work_dirty_ = false;
+    ensure_nlist();
     drop_graph();
+}
+
+// Neighbour lists for variant bit 3, sized to the particle arena.  Without
+// room in the HBM budget the variant runs without them (bit 3 ignored).
+void System::ensure_nlist() {
+    nl_ready_ = false;
+    if (!(cfg_.variant & 8) || !any_fast_) {
+        if (nlist_.n) {
+            nlist_.release();
+            ncnt_.release();
+            drop_graph();
+        }
+        return;
+    }
+    const int64_t slots = (int64_t)kNbCap * pos_.n;
+    if (nlist_.n != slots || ncnt_.n != pos_.n) {
+        const int64_t extra = (slots - nlist_.n) * 4 + (pos_.n - ncnt_.n) * 4;
+        if (cfg_.hbm_budget > 0 && memory_bytes() + extra > cfg_.hbm_budget) return;
+        nlist_.resize(slots, false, st_);
+        ncnt_.resize(pos_.n, false, st_);
+        drop_graph();
+    }
+    nl_ready_ = true;
 }
 
 DevArrays System::arrays() const {
@@ -869,6 +896,9 @@ DevArrays System::arrays() const {
     a.nbid = nbid_.p;
     a.snbid = snbid_.p;
     a.rec = rec_.p;
+    a.nlist = nlist_.p;
+    a.ncnt = ncnt_.p;
+    a.nl_stride = pos_.n;
     a.counts = counts_.p;
     a.offsets = offsets_.p;
     a.chunk_sum = chunk_.p;
@@ -886,7 +916,7 @@ LaunchShape System::shape() const {
     s.grid_p = n_ptiles_;
     s.grid_c = n_ctiles_;
     s.grid_t = n_ttiles_;
-    s.variant = cfg_.variant;
+    s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~8);
     return s;
 }
 
@@ -1145,7 +1175,7 @@ void System::autotune(int steps, sph_tune_result* out) {
     };
     const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
-    const int variants[4] = {0, 1, 4, 5};
+    const int variants[] = {0, 1, 4, 8, 12};
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;
     float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;

@@ -126,6 +126,7 @@ class System {
     void grow_tables(int64_t cap);
     void grow_chunks(int64_t cap);
     void rebuild_work();
+    void ensure_nlist();
     DevArrays arrays() const;
     LaunchShape shape() const;
     void enqueue_step(const DevArrays& a, const LaunchShape& s, cudaEvent_t* ev);
@@ -147,6 +148,9 @@ class System {
     DevBuf<uint32_t> key_, slot_, perm_;
     DevBuf<int32_t> nbid_, snbid_;
     DevBuf<float> rec_;
+    DevBuf<uint32_t> nlist_;  // kNbCap slots per arena particle (variant bit 3)
+    DevBuf<int32_t> ncnt_;
+    bool nl_ready_ = false;
     // key arena
     DevBuf<uint32_t> counts_, offsets_;
     DevBuf<uint32_t> chunk_;

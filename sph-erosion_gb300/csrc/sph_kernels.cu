@@ -608,7 +608,7 @@ __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
 // LISTED: the in-range pairs are compacted (for_each_in_range_listed) instead
 // of evaluated inside the candidate loop; which one is faster depends on the
 // neighbour density, so the autotuner picks it.
-template <bool ORDERED, bool LISTED, int MINB>
+template <bool ORDERED, bool LISTED, int MINB, bool NL = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
@@ -637,10 +637,25 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
             });
             if (!valid) continue;
         } else {
-            for_each_candidate(a, S, xi, [&](uint32_t, float4 xj) {
+            // NL: the in-range candidates, in visiting order, also go to the
+            // particle's neighbour list for the force pass
+            uint32_t* nl = a.nlist + p;
+            const int64_t stride = a.nl_stride;
+            int cnt = 0;
+            for_each_candidate(a, S, xi, [&](uint32_t j, float4 xj) {
                 const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
-                if (s <= S.smax) rho = fa(rho, density_term(S, fsq(s)));
+                if (s <= S.smax) {
+                    rho = fa(rho, density_term(S, fsq(s)));
+                    if (NL) {
+                        if (cnt < kNbCap) {
+                            *nl = j;
+                            nl += stride;
+                        }
+                        ++cnt;
+                    }
+                }
             });
+            if (NL) a.ncnt[p] = cnt;
         }
         const float P = fm(S.k, fs(rho, S.p0));
         a.dyn[p] = make_float4(rho, fdv(P, fm(rho, rho)), fdv(S.mass, rho), P);
@@ -649,7 +664,10 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
 
 // force: passes 2 and 3 (fluid_system.h:127-178) and advance (:306-353) with
 // the terrain contact, the box collision and the erosion exchange.
-template <bool ORDERED, int MINB>
+// NL: the in-range neighbours come from the lists the density pass wrote
+// (same order as the traversal, so the same sums); a warp with a particle
+// whose list overflowed traverses the cells as without lists.
+template <bool ORDERED, int MINB, bool NL = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
@@ -683,7 +701,17 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
             // the ordered list holds only in-range candidates
             if (!for_each_in_range_ordered(a, S, xi, pair)) atomicOr(a.status, 1u);
         } else {
-            for_each_in_range_listed(a, S, valid, xi, list, [&](uint32_t j) { pair(j, __ldg(sp + j)); });
+            const int cnt = (NL && valid) ? a.ncnt[p] : 0;
+            if (!NL || __any_sync(kFull, cnt > kNbCap)) {
+                for_each_in_range_listed(a, S, valid, xi, list, [&](uint32_t j) { pair(j, __ldg(sp + j)); });
+            } else {
+                const uint32_t* nl = a.nlist + p;
+                const int64_t stride = a.nl_stride;
+                for (int q = 0; q < cnt; ++q, nl += stride) {
+                    const uint32_t j = __ldg(nl);
+                    pair(j, __ldg(sp + j));
+                }
+            }
             if (!valid) continue;
         }
         // pass-2 results (:151-154) and pass 3 (:163, :177)
@@ -946,15 +974,24 @@ void configure_kernels() {
     cudaFuncSetAttribute(k_density<false, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.tile * sizeof(uint32_t); }
 
 // Variant bit 2 relaxes the register budget of the two neighbour kernels
 // (fewer resident blocks, no spills) against the default high occupancy.
+// Bit 3 hands the in-range neighbour lists from the density pass to the force
+// pass (takes precedence over bit 0).
 void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     const bool relaxed = (s.variant & 4) != 0;
-    if (s.variant & 1) {
+    if (s.variant & 8) {
+        if (relaxed)
+            k_density<false, false, 4, true><<<s.grid_p, s.tile, 0, st>>>(a);
+        else
+            k_density<false, false, 8, true><<<s.grid_p, s.tile, 0, st>>>(a);
+    } else if (s.variant & 1) {
         if (relaxed)
             k_density<false, true, 4><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
         else
@@ -970,7 +1007,12 @@ void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream
     k_density<true, false, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    if (s.variant & 4)
+    if (s.variant & 8) {
+        if (s.variant & 4)
+            k_force<false, 3, true><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+        else
+            k_force<false, 4, true><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+    } else if (s.variant & 4)
         k_force<false, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
     else
         k_force<false, 4><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);

@@ -39,16 +39,26 @@ struct DevArrays {
     const float* tbase;
     long long* tdelta;
     float* theight;
+    // in-range neighbour lists written by the density pass and read by the
+    // force pass (variant bit 3): slot q of sorted particle p at
+    // nlist[q * nl_stride + p], in traversal order; ncnt[p] = in-range count
+    // (may exceed kNbCap: the force pass then traverses the cells again)
+    uint32_t* nlist;
+    int32_t* ncnt;
+    int64_t nl_stride;
     // status word: bit 0 = ordered-mode neighbour overflow
     unsigned* status;
 };
+
+// Slots per particle of the in-range neighbour lists.
+constexpr int kNbCap = 64;
 
 struct LaunchShape {
     int tile;        // threads per particle tile
     int grid_p;      // persistent grid of particle kernels
     int grid_c;      // persistent grid of the scan
     int grid_t;      // persistent grid of the terrain kernel
-    int variant;     // sph_system_config.variant bits
+    int variant;     // sph_system_config.variant bits (bit 3 only with lists allocated)
 };
 
 // Once per process and device: opt the list-traversal kernels into >48 KB of

@@ -97,8 +97,8 @@ class ServerConfig(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("tile", C.c_int), ("cell_mult", C.c_float), ("variant", C.c_int), ("ms_per_step", C.c_float),
-                ("n_tried", C.c_int), ("tiles", C.c_int * 16), ("cell_mults", C.c_float * 16),
-                ("variants", C.c_int * 16), ("ms", C.c_float * 16)]
+                ("n_tried", C.c_int), ("tiles", C.c_int * 32), ("cell_mults", C.c_float * 32),
+                ("variants", C.c_int * 32), ("ms", C.c_float * 32)]
 
     def as_dict(self):
         return {"tile": self.tile, "cell_mult": self.cell_mult, "variant": self.variant,
@@ -297,12 +297,14 @@ def params_dict(p: Params) -> dict:
 
 class System:
     def __init__(self, particle_capacity=1 << 16, key_capacity=1 << 16, terrain_capacity=1 << 12, max_scenes=1024,
-                 tile=256, graph_steps=16, hbm_budget=0, device=0):
+                 tile=256, graph_steps=16, hbm_budget=0, device=0, variant=None):
         cfg = SystemConfig()
         lib().sph_system_config_default(C.byref(cfg))
         cfg.device, cfg.particle_capacity, cfg.key_capacity = device, particle_capacity, key_capacity
         cfg.terrain_capacity, cfg.max_scenes, cfg.tile = terrain_capacity, max_scenes, tile
         cfg.graph_steps, cfg.hbm_budget = graph_steps, hbm_budget
+        if variant is not None:
+            cfg.variant = variant
         h = C.c_void_p()
         _ck(lib().sph_system_create(C.byref(cfg), C.byref(h)))
         self.h = h

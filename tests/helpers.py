@@ -22,9 +22,10 @@ FIELDS = {"pos": slice(0, 3), "vel": slice(3, 6), "acc": slice(6, 9), "density":
 RTOL = 1e-4
 
 
-def run(params: dict, pos, steps, vel=None, flags=S.SPH_FLAG_RECORD, graph_steps=16, tile=256, cell_mult=1.0):
+def run(params: dict, pos, steps, vel=None, flags=S.SPH_FLAG_RECORD, graph_steps=16, tile=256, cell_mult=1.0,
+        variant=None):
     """Run `steps` (int or list of step counts) and return {steps: (rec, nbid)}."""
-    with S.System(particle_capacity=max(len(pos), 1), graph_steps=graph_steps, tile=tile) as sysm:
+    with S.System(particle_capacity=max(len(pos), 1), graph_steps=graph_steps, tile=tile, variant=variant) as sysm:
         sc = sysm.scene(S.default_params(**params, flags=flags, cell_mult=cell_mult), capacity=len(pos))
         sc.set_particles(pos, vel)
         out = {}
