@@ -188,7 +188,7 @@ def run_ours(args, spec, config):
     torch.cuda.set_device(local)
     n = spec["n"]
     sysm = S.System(particle_capacity=n, key_capacity=1 << 20, terrain_capacity=1 << 21, tile=args.tile,
-                    graph_steps=16, device=local)
+                    graph_steps=16, device=local, variant=args.variant)
     spec = dict(spec, params=dict(spec["params"], cell_mult=args.cell_mult))
     sc = W.build_scene(sysm, spec)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
@@ -307,7 +307,7 @@ def run_batched(args, config):
     total_all = sum(r["particles"] for r in all_reqs)
     base = W.base_params(args.cell_mult)
     sysm = S.System(particle_capacity=total + 512 * len(reqs), key_capacity=1 << 24, terrain_capacity=1 << 24,
-                    tile=args.tile, graph_steps=16, device=local)
+                    tile=args.tile, graph_steps=16, device=local, variant=args.variant)
     for r in reqs:
         sysm.scene_from_request(base, r)
     sysm.step(args.warmup)
@@ -320,9 +320,11 @@ def run_batched(args, config):
     # plain form: one system per scene, same steps, same tuned tile and cell
     tile = tuned["tile"] if tuned else args.tile
     cm = tuned["cell_mult"] if tuned else args.cell_mult
+    variant = tuned["variant"] if tuned else args.variant
     plain_ms = 0.0
     for r in reqs:
-        with S.System(particle_capacity=r["particles"], tile=tile, graph_steps=16, device=local) as one:
+        with S.System(particle_capacity=r["particles"], tile=tile, graph_steps=16, device=local,
+                      variant=variant) as one:
             one.scene_from_request(W.base_params(cm), r)
             one.step(args.warmup)
             one.sync()
@@ -397,6 +399,8 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep --tile/--cell-mult instead of autotuning them")
     ap.add_argument("--tile", type=int, default=256)
+    ap.add_argument("--variant", type=int, default=None,
+                    help="kernel variant bits of the plain workloads (before autotuning)")
     ap.add_argument("--cell-mult", type=float, default=0.5)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")

@@ -113,7 +113,11 @@ typedef struct sph_system_config {
                                  8 = the density pass writes each particle's in-range
                                      neighbours (64 slots, 260 B per particle) and the
                                      force pass reads them instead of re-testing the
-                                     cells; ignored when the HBM budget has no room */
+                                     cells; ignored when the HBM budget has no room,
+                                16 = with 8: the force pass's list walk loads ahead,
+                                32 = with 8: middle register budget of the density pass,
+                                64 = with 8: the density pass loads candidates in pairs;
+                                default 88 (8 + 16 + 64) */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;
 

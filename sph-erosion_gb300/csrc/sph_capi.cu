@@ -85,6 +85,7 @@ void sph_system_config_default(sph_system_config* c) {
     c->max_scenes = 1024;
     c->tile = 256;
     c->graph_steps = 16;
+    c->variant = 88;  // neighbour lists, pipelined list walk, paired candidate loads
     c->hbm_budget = 0;
 }
 

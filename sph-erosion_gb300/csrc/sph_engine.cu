@@ -916,7 +916,7 @@ LaunchShape System::shape() const {
     s.grid_p = n_ptiles_;
     s.grid_c = n_ctiles_;
     s.grid_t = n_ttiles_;
-    s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~8);
+    s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~120);
     return s;
 }
 
@@ -1175,7 +1175,7 @@ void System::autotune(int steps, sph_tune_result* out) {
     };
     const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
-    const int variants[] = {0, 1, 4, 8, 12};
+    const int variants[] = {0, 4, 24, 28, 88};
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;
     float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;

@@ -229,6 +229,22 @@ __device__ __forceinline__ void for_each_candidate(const DevArrays& a, const Sce
     });
 }
 
+// The same visit with the candidates of a row taken two at a time (both
+// loads issued before either is tested); the order is unchanged.
+template <class F>
+__device__ __forceinline__ void for_each_candidate_x2(const DevArrays& a, const SceneDev& S, float4 xi, F&& f) {
+    const float4* sp = a.spos + S.p_off;
+    for_rows(a, S, xi, true, [&](uint32_t st, uint32_t en) {
+        uint32_t j = st;
+        for (; j + 1 < en; j += 2) {
+            const float4 x0 = __ldg(sp + j), x1 = __ldg(sp + j + 1);
+            f(j, x0);
+            f(j + 1, x1);
+        }
+        if (j < en) f(j, __ldg(sp + j));
+    });
+}
+
 // In-range traversal of the fast path.  Candidates are tested in a tight
 // loop and the indices of in-range ones are compacted into a per-thread list
 // in shared memory (column threadIdx.x, so lanes touch distinct banks); the
@@ -442,12 +458,30 @@ __device__ __forceinline__ bool box_collide(const SceneDev& S, float px, float p
 __device__ __forceinline__ float len3(float x, float y, float z) { return fsq(dist2(x, y, z)); }
 
 // ---------------------------------------------------------------------------
-// keys: cell key of each particle, its slot within the cell (warp-aggregated
+// Runs of equal values among the valid lanes of a warp (the valid lanes are a
+// prefix, `mask`): the first lane of each run adds the run's length to
+// counter[v] and every lane gets old value + its position in the run.  The
+// state arrives in the previous step's sorted order, so particles of one cell
+// are mostly adjacent and one atomic serves each cell.
+__device__ __forceinline__ uint32_t run_aggregated_add(uint32_t* counter, uint32_t v, unsigned mask, int lane) {
+    const uint32_t prev = __shfl_up_sync(mask, v, 1);
+    const bool start = lane == 0 || prev != v;
+    const unsigned starts = __ballot_sync(mask, start);
+    const unsigned upto = (2u << lane) - 1u;  // lanes 0..lane (all lanes for lane 31)
+    const int leader = 31 - __clz(starts & upto);
+    const unsigned above = starts & ~upto;
+    const int end = above ? __ffs(above) - 1 : 32 - __clz(mask);
+    uint32_t base = 0;
+    if (start) base = atomicAdd(counter + v, (uint32_t)(end - lane));
+    base = __shfl_sync(mask, base, leader);
+    return base + (uint32_t)(lane - leader);
+}
+
+// keys: cell key of each particle, its slot within the cell (run-aggregated
 // atomics) and the per-chunk totals that the scan needs.
 __global__ void __launch_bounds__(kMaxTile) k_keys(DevArrays a) {
     const int nwork = *a.n_ptiles;
     const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = a.ptiles[w];
         if (a.steps_left[wk.scene] == 0) continue;
@@ -459,17 +493,10 @@ __global__ void __launch_bounds__(kMaxTile) k_keys(DevArrays a) {
         const float4 x = a.pos[i];
         const Cell c = cell_of(S, x.x, x.y, x.z);
         const uint32_t k = row_key(a.tab, S, c.cy, c.cz) + (uint32_t)c.cx;
-        const uint32_t gk = (uint32_t)S.k_off + k;
-        const unsigned peers = __match_any_sync(mask, gk);
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(a.counts + gk, (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader);
+        const uint32_t slot = run_aggregated_add(a.counts, (uint32_t)S.k_off + k, mask, lane);
         a.key[i] = k;
-        a.slot[i] = base + (uint32_t)__popc(peers & lt);
-        const uint32_t ck = (uint32_t)S.c_off + (k >> kChunkBits);
-        const unsigned cpeers = __match_any_sync(mask, ck);
-        if (lane == __ffs(cpeers) - 1) atomicAdd(a.chunk_sum + ck, (uint32_t)__popc(cpeers));
+        a.slot[i] = slot;
+        run_aggregated_add(a.chunk_sum, (uint32_t)S.c_off + (k >> kChunkBits), mask, lane);
     }
 }
 
@@ -608,14 +635,14 @@ __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
 // LISTED: the in-range pairs are compacted (for_each_in_range_listed) instead
 // of evaluated inside the candidate loop; which one is faster depends on the
 // neighbour density, so the autotuner picks it.
-template <bool ORDERED, bool LISTED, int MINB, bool NL = false>
+template <bool ORDERED, bool LISTED, int MINB, bool NL = false, bool X2 = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = a.ptiles[w];
         if (a.steps_left[wk.scene] == 0) continue;
-        const SceneDev& S = a.scenes[wk.scene];
+        const SceneDev S = a.scenes[wk.scene];  // by value: the list stores cannot alias it
         if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
         const int p = wk.start + threadIdx.x;
         const bool valid = p < S.p_off + S.n;
@@ -642,7 +669,7 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
             uint32_t* nl = a.nlist + p;
             const int64_t stride = a.nl_stride;
             int cnt = 0;
-            for_each_candidate(a, S, xi, [&](uint32_t j, float4 xj) {
+            auto visit = [&](uint32_t j, float4 xj) {
                 const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
                 if (s <= S.smax) {
                     rho = fa(rho, density_term(S, fsq(s)));
@@ -654,7 +681,11 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
                         ++cnt;
                     }
                 }
-            });
+            };
+            if (X2)
+                for_each_candidate_x2(a, S, xi, visit);
+            else
+                for_each_candidate(a, S, xi, visit);
             if (NL) a.ncnt[p] = cnt;
         }
         const float P = fm(S.k, fs(rho, S.p0));
@@ -666,8 +697,10 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
 // the terrain contact, the box collision and the erosion exchange.
 // NL: the in-range neighbours come from the lists the density pass wrote
 // (same order as the traversal, so the same sums); a warp with a particle
-// whose list overflowed traverses the cells as without lists.
-template <bool ORDERED, int MINB, bool NL = false>
+// whose list overflowed traverses the cells as without lists.  NL = 2
+// software-pipelines the list walk: list entries two ahead and the
+// neighbour's state one ahead are loaded before the current pair is summed.
+template <bool ORDERED, int MINB, int NL = 0>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
@@ -689,14 +722,13 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
         const float4* sp = a.spos + S.p_off;
         const float4* sv = a.svel + S.p_off;
         const float4* sd = a.dyn + S.p_off;
-        auto pair = [&](uint32_t j, float4 xj) {
+        auto pair_with = [&](uint32_t j, float4 xj, float4 vj, float4 dj) {
             const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
             const float s = dist2(rx, ry, rz);
-            const float4 vj = __ldg(sv + j);
-            const float4 dj = __ldg(sd + j);
             force_pair(S, acc, rx, ry, rz, fsq(s), vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z, __float_as_int(xj.w),
                        (int)j == pl);
         };
+        auto pair = [&](uint32_t j, float4 xj) { pair_with(j, xj, __ldg(sv + j), __ldg(sd + j)); };
         if (ORDERED) {
             // the ordered list holds only in-range candidates
             if (!for_each_in_range_ordered(a, S, xi, pair)) atomicOr(a.status, 1u);
@@ -704,12 +736,39 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
             const int cnt = (NL && valid) ? a.ncnt[p] : 0;
             if (!NL || __any_sync(kFull, cnt > kNbCap)) {
                 for_each_in_range_listed(a, S, valid, xi, list, [&](uint32_t j) { pair(j, __ldg(sp + j)); });
-            } else {
+            } else if (NL == 1) {
                 const uint32_t* nl = a.nlist + p;
                 const int64_t stride = a.nl_stride;
                 for (int q = 0; q < cnt; ++q, nl += stride) {
                     const uint32_t j = __ldg(nl);
                     pair(j, __ldg(sp + j));
+                }
+            } else {
+                const uint32_t* nl = a.nlist + p;
+                const int64_t stride = a.nl_stride;
+                uint32_t j0 = cnt > 0 ? __ldg(nl) : 0u;
+                uint32_t j1 = cnt > 1 ? __ldg(nl + stride) : 0u;
+                float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), v0 = x0, d0 = x0;
+                if (cnt > 0) {
+                    x0 = __ldg(sp + j0);
+                    v0 = __ldg(sv + j0);
+                    d0 = __ldg(sd + j0);
+                }
+                nl += 2 * stride;
+                for (int q = 0; q < cnt; ++q, nl += stride) {
+                    const uint32_t j2 = (q + 2 < cnt) ? __ldg(nl) : 0u;
+                    float4 x1 = x0, v1 = v0, d1 = d0;
+                    if (q + 1 < cnt) {
+                        x1 = __ldg(sp + j1);
+                        v1 = __ldg(sv + j1);
+                        d1 = __ldg(sd + j1);
+                    }
+                    pair_with(j0, x0, v0, d0);
+                    j0 = j1;
+                    j1 = j2;
+                    x0 = x1;
+                    v0 = v1;
+                    d0 = d1;
                 }
             }
             if (!valid) continue;
@@ -974,8 +1033,10 @@ void configure_kernels() {
     cudaFuncSetAttribute(k_density<false, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.tile * sizeof(uint32_t); }
@@ -983,12 +1044,18 @@ static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.til
 // Variant bit 2 relaxes the register budget of the two neighbour kernels
 // (fewer resident blocks, no spills) against the default high occupancy.
 // Bit 3 hands the in-range neighbour lists from the density pass to the force
-// pass (takes precedence over bit 0).
+// pass (takes precedence over bit 0); bit 4 with it pipelines the force
+// pass's list walk; bit 5 with it gives the density pass a middle register
+// budget (6 resident blocks of 256 threads).
 void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     const bool relaxed = (s.variant & 4) != 0;
     if (s.variant & 8) {
         if (relaxed)
             k_density<false, false, 4, true><<<s.grid_p, s.tile, 0, st>>>(a);
+        else if (s.variant & 32)
+            k_density<false, false, 6, true><<<s.grid_p, s.tile, 0, st>>>(a);
+        else if (s.variant & 64)
+            k_density<false, false, 8, true, true><<<s.grid_p, s.tile, 0, st>>>(a);
         else
             k_density<false, false, 8, true><<<s.grid_p, s.tile, 0, st>>>(a);
     } else if (s.variant & 1) {
@@ -1007,11 +1074,16 @@ void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream
     k_density<true, false, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    if (s.variant & 8) {
+    if ((s.variant & 24) == 24) {
         if (s.variant & 4)
-            k_force<false, 3, true><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 3, 2><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
         else
-            k_force<false, 4, true><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 4, 2><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+    } else if (s.variant & 8) {
+        if (s.variant & 4)
+            k_force<false, 3, 1><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+        else
+            k_force<false, 4, 1><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
     } else if (s.variant & 4)
         k_force<false, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
     else
