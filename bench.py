@@ -240,13 +240,16 @@ def run_ours(args, spec, config):
     ncells = int(np.prod(sc.grid_dims()[:3]))
     step_bytes = 88.0 * n + 16.0 * ncells + 20.0 * texels
     cpu_v, cores, m, _ = cpu_sample(spec, budget_s=args.ref_seconds)
+    variant = tuned["variant"] if tuned else args.variant if args.variant is not None else 88
+    cm = tuned["cell_mult"] if tuned else args.cell_mult
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + fBm terrain)",
         "config": config,
         "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_kind": kind,
+                     "frac": achieved / hbm, "traffic": NCU_FORCE_TRAFFIC.get((config["workload"], variant, cm)),
+                     "peak_kind": kind,
                      "step_bytes_frac": step_bytes / (step_ms * 1e-3) / 1e9 / hbm},
         "cpu_baseline": {"value": cpu_v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{m} of {n} particles x 3 all-pairs passes + integration per step"},
@@ -265,6 +268,11 @@ def run_ours(args, spec, config):
 
 
 C_PARAMS_BYTES = 4 * 24
+
+# DRAM bytes (read + write) of one k_force launch, from an ncu capture of the
+# same workload with kernel variant 88 and cell_mult 0.5 (the neighbour lists
+# the force pass reads are most of it).  Reported only for that configuration.
+NCU_FORCE_TRAFFIC = {("plain_1m", 88, 0.5): 210.7e6}
 
 
 def _init_ranks():
@@ -406,6 +414,7 @@ def main():
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="serving: requests in the trace")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
+    ap.add_argument("--particles", type=int, default=8388608, help="skew: particles (the box floor scales with them)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="warm-up and timed steps only (for profiler captures); prints nothing")
     args = ap.parse_args()
@@ -415,7 +424,7 @@ def main():
         cfg = {"h": W.H, "dt": W.PHYS["dt"], "erosion": True, "tile": args.tile, "cell_mult": args.cell_mult}
         (run_batched if args.workload == "batched" else run_serving)(args, cfg)
         return
-    spec = {"plain_small": W.plain_small, "skew": W.skew_rain}.get(args.workload, W.plain_1m)()
+    spec = {"plain_small": W.plain_small, "skew": lambda: W.skew_rain(args.particles)}.get(args.workload, W.plain_1m)()
     t = spec.get("terrain")
     config = {"workload": spec["name"], "particles": spec["n"],
               "terrain": f"{t['w']}x{t['d']} fBm {t['octaves']} oct amp {t['amplitude']}" if t else None,

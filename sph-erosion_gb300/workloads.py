@@ -72,14 +72,18 @@ def scaled_block(n, box_half=(0.5, 0.5, 0.5), amp=0.2):
     return lattice_block(nx, ny, nz, SPACING, lo, limit=n)
 
 
-def skew_rain(n=8388608, seed=5, terrain_side=4096):
+def skew_rain(n=8388608, seed=5, terrain_side=None):
     """Skewed-occupancy stress: n particles released as rainfall (x, z uniform
     over the box floor, y uniform in the top 10% of the box height) over a
     terrain_side^2 carved-valley terrain (inverted ridged fBm, 6 octaves,
-    amplitude 0.5), at rest.  The box (16 x 2 x 16 m) makes the rain layer's
-    mean density about 1.3x the rest density; the rain then pools in the
-    valleys into very uneven cell occupancy."""
-    box_half = (8.0, 1.0, 8.0)
+    amplitude 0.5), at rest.  The box (16 x 2 x 16 m at n = 8,388,608, its
+    floor scaled with n otherwise) makes the rain layer's mean density about
+    1.3x the rest density; the rain then pools in the valleys into very
+    uneven cell occupancy.  The terrain keeps 4096 vertices per 16 m."""
+    f = float(np.sqrt(n / 8388608.0))
+    box_half = (8.0 * f, 1.0, 8.0 * f)
+    if terrain_side is None:
+        terrain_side = max(64, int(round(4096 * f)))
     rng = np.random.default_rng(seed)
     pos = np.empty((n, 3), np.float32)
     pos[:, 0] = rng.uniform(-box_half[0] + SPACING / 2, box_half[0] - SPACING / 2, n)
