@@ -7,9 +7,8 @@
 // batched query.  Every operation is an explicitly rounded FP32 intrinsic in
 // the reference's order, so results equal the reference's bit for bit.
 //
-// Two deliberate departures, both where the reference reads outside its map
-// (undefined behaviour): a height lookup outside [0, 511] reads 0, and
-// cells are addressed by the integer value of their float index.
+// One deliberate departure, where the reference reads outside its map
+// (undefined behaviour): a height lookup outside [0, 511] reads 0.
 #include <cuda_runtime.h>
 
 #include <cmath>
