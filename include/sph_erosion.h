@@ -116,7 +116,9 @@ typedef struct sph_system_config {
                                      cells; ignored when the HBM budget has no room,
                                 16 = with 8: the force pass's list walk loads ahead,
                                 32 = with 8: middle register budget of the density pass,
-                                64 = with 8: the density pass loads candidates in pairs;
+                                64 = with 8: the density pass loads candidates in pairs,
+                               128 = with 8: the force pass gathers one packed 32-byte
+                                     record per neighbour (32 more bytes per particle);
                                 default 88 (8 + 16 + 64) */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;

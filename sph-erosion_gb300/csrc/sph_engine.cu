@@ -17,6 +17,9 @@ namespace {
 
 constexpr int kPAlign = kRangeAlign;  // particle ranges start on a tile boundary for every tile size
 constexpr int64_t kTAlign = kRangeAlign;
+// Largest arena size in entries: offsets and in-scene indices stay inside the
+// kernels' 32-bit index arithmetic with room for a tile of overrun.
+constexpr int64_t kMaxArenaIndex = ((int64_t)1 << 31) - ((int64_t)1 << 20);
 
 int64_t round_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
@@ -164,6 +167,9 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
     if (cfg_.tile == 0) cfg_.tile = 256;
     if (cfg_.tile != 128 && cfg_.tile != 256) throw Error(SPH_ERR_INVALID, "tile must be 128 or 256");
     if (cfg_.max_scenes <= 0) cfg_.max_scenes = 1024;
+    if (cfg_.particle_capacity > kMaxArenaIndex || cfg_.key_capacity > kMaxArenaIndex ||
+        cfg_.terrain_capacity > kMaxArenaIndex)
+        throw Error(SPH_ERR_INVALID, "capacities are limited to 2^31 - 2^20 entries");
     dev_ = cfg_.device;
     SPH_CK(cudaSetDevice(dev_));
     SPH_CK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
@@ -197,7 +203,7 @@ System::~System() {
     for (auto* b : f4) b->release();
     key_.release(); slot_.release(); perm_.release();
     nbid_.release(); snbid_.release(); rec_.release();
-    nlist_.release(); ncnt_.release();
+    nlist_.release(); ncnt_.release(); fdat_.release();
     counts_.release(); offsets_.release(); chunk_.release(); tab_.release();
     tbase_.release(); theight_.release(); tdelta_.release();
     dscenes_.release(); steps_.release(); ptiles_.release(); ctiles_.release(); ttiles_.release();
@@ -219,7 +225,7 @@ int64_t System::memory_bytes() const {
     int64_t b = 0;
     b += pos_.bytes() + vel_.bytes() + spos_.bytes() + svel_.bytes() + dyn_.bytes();
     b += key_.bytes() + slot_.bytes() + perm_.bytes() + nbid_.bytes() + snbid_.bytes() + rec_.bytes();
-    b += nlist_.bytes() + ncnt_.bytes();
+    b += nlist_.bytes() + ncnt_.bytes() + fdat_.bytes();
     b += counts_.bytes() + offsets_.bytes() + chunk_.bytes() + tab_.bytes();
     b += tbase_.bytes() + theight_.bytes() + tdelta_.bytes();
     b += dscenes_.bytes() + steps_.bytes() + ptiles_.bytes() + ctiles_.bytes() + ttiles_.bytes();
@@ -233,7 +239,8 @@ int64_t System::scene_bytes(int n, int tw, int td, const sph_params& p) const {
     tmp.prm = p;
     const_cast<System*>(this)->geometry(tmp);
     const int64_t pcap = round_up(std::max(n, 1), kPAlign);
-    const int64_t per_p = 5 * 16 + 3 * 4 + 2 * 4 + ((p.flags & SPH_FLAG_RECORD) ? kRecFloats * 4 : 0);
+    int64_t per_p = 5 * 16 + 3 * 4 + 2 * 4 + ((p.flags & SPH_FLAG_RECORD) ? kRecFloats * 4 : 0);
+    if (cfg_.variant & 8) per_p += (int64_t)kNbCap * 4 + 4 + ((cfg_.variant & 128) ? 32 : 0);  // neighbour lists
     return pcap * per_p + (int64_t)tmp.k_cap * 8 + (int64_t)tmp.nchunks * 4 + tmp.tab_len * 4 +
            round_up((int64_t)tw * td, kTAlign) * 16 + (int64_t)(pcap / cfg_.tile + tmp.nchunks) * 8;
 }
@@ -297,22 +304,30 @@ void System::grow_terrain(int64_t cap) {
     drop_graph();
 }
 
-// which: 0 particles, 1 keys, 2 chunks, 3 tables, 4 terrain
+// which: 0 particles, 1 keys, 2 chunks, 3 tables, 4 terrain.  Every arena
+// stays below kMaxArenaIndex entries: the kernels index them with 32-bit
+// offsets (a particle, key or vertex offset plus an index within the scene).
+// A scene that would need more gets SPH_ERR_CAPACITY (a server waits for
+// retirements).
 void System::ensure_arena(RangeAlloc& ra, int64_t need, int which) {
     int64_t off;
     if (ra.alloc(need, &off)) {
         ra.release(off, need);
         return;
     }
+    const int64_t align = which == 0 ? kPAlign : which == 1 ? kChunk : which == 4 ? kTAlign : 1;
+    const int64_t limit = kMaxArenaIndex / align * align;
+    if (ra.cap() + need > limit) throw Error(SPH_ERR_CAPACITY, "arena index range exhausted (2^31 entries)");
     // Double the arena; under an HBM budget fall back to growing by exactly
     // what is missing when doubling would not fit.
     auto grow = [&](int64_t cap) {
+        cap = std::min(round_up(cap, align), limit);
         switch (which) {
-            case 0: grow_particles(round_up(cap, kPAlign)); break;
-            case 1: grow_keys(round_up(cap, kChunk)); break;
+            case 0: grow_particles(cap); break;
+            case 1: grow_keys(cap); break;
             case 2: grow_chunks(cap); break;
             case 3: grow_tables(cap); break;
-            default: grow_terrain(round_up(cap, kTAlign)); break;
+            default: grow_terrain(cap); break;
         }
     };
     const int64_t doubled = std::max(ra.cap() * 2, ra.cap() + need);
@@ -856,19 +871,25 @@ void System::rebuild_work() {
 void System::ensure_nlist() {
     nl_ready_ = false;
     if (!(cfg_.variant & 8) || !any_fast_) {
-        if (nlist_.n) {
+        if (nlist_.n || fdat_.n) {
             nlist_.release();
             ncnt_.release();
+            fdat_.release();
             drop_graph();
         }
         return;
     }
     const int64_t slots = (int64_t)kNbCap * pos_.n;
-    if (nlist_.n != slots || ncnt_.n != pos_.n) {
-        const int64_t extra = (slots - nlist_.n) * 4 + (pos_.n - ncnt_.n) * 4;
+    const int64_t recs = (cfg_.variant & 128) ? 2 * pos_.n : 0;
+    if (nlist_.n != slots || ncnt_.n != pos_.n || fdat_.n != recs) {
+        const int64_t extra = (slots - nlist_.n) * 4 + (pos_.n - ncnt_.n) * 4 + (recs - fdat_.n) * 16;
         if (cfg_.hbm_budget > 0 && memory_bytes() + extra > cfg_.hbm_budget) return;
         nlist_.resize(slots, false, st_);
         ncnt_.resize(pos_.n, false, st_);
+        if (recs)
+            fdat_.resize(recs, false, st_);
+        else
+            fdat_.release();
         drop_graph();
     }
     nl_ready_ = true;
@@ -899,6 +920,7 @@ DevArrays System::arrays() const {
     a.nlist = nlist_.p;
     a.ncnt = ncnt_.p;
     a.nl_stride = pos_.n;
+    a.fdat = fdat_.p;
     a.counts = counts_.p;
     a.offsets = offsets_.p;
     a.chunk_sum = chunk_.p;
@@ -916,7 +938,7 @@ LaunchShape System::shape() const {
     s.grid_p = n_ptiles_;
     s.grid_c = n_ctiles_;
     s.grid_t = n_ttiles_;
-    s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~120);
+    s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~248);
     return s;
 }
 
@@ -1175,7 +1197,7 @@ void System::autotune(int steps, sph_tune_result* out) {
     };
     const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
-    const int variants[] = {0, 4, 24, 28, 88};
+    const int variants[] = {0, 4, 28, 88, 216};
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;
     float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;

@@ -150,6 +150,7 @@ class System {
     DevBuf<float> rec_;
     DevBuf<uint32_t> nlist_;  // kNbCap slots per arena particle (variant bit 3)
     DevBuf<int32_t> ncnt_;
+    DevBuf<float4> fdat_;     // 2 per arena particle (variant bit 7)
     bool nl_ready_ = false;
     // key arena
     DevBuf<uint32_t> counts_, offsets_;

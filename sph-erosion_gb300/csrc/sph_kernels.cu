@@ -462,41 +462,85 @@ __device__ __forceinline__ float len3(float x, float y, float z) { return fsq(di
 // prefix, `mask`): the first lane of each run adds the run's length to
 // counter[v] and every lane gets old value + its position in the run.  The
 // state arrives in the previous step's sorted order, so particles of one cell
-// are mostly adjacent and one atomic serves each cell.
-__device__ __forceinline__ uint32_t run_aggregated_add(uint32_t* counter, uint32_t v, unsigned mask, int lane) {
+// are mostly adjacent and one atomic serves each cell.  Split in three phases
+// so that several independent runs can have their atomics in flight at once.
+struct Run {
+    bool start;
+    int leader;
+    uint32_t len;
+};
+
+__device__ __forceinline__ Run run_of(uint32_t v, unsigned mask, int lane) {
     const uint32_t prev = __shfl_up_sync(mask, v, 1);
-    const bool start = lane == 0 || prev != v;
-    const unsigned starts = __ballot_sync(mask, start);
+    Run r;
+    r.start = lane == 0 || prev != v;
+    const unsigned starts = __ballot_sync(mask, r.start);
     const unsigned upto = (2u << lane) - 1u;  // lanes 0..lane (all lanes for lane 31)
-    const int leader = 31 - __clz(starts & upto);
+    r.leader = 31 - __clz(starts & upto);
     const unsigned above = starts & ~upto;
     const int end = above ? __ffs(above) - 1 : 32 - __clz(mask);
-    uint32_t base = 0;
-    if (start) base = atomicAdd(counter + v, (uint32_t)(end - lane));
-    base = __shfl_sync(mask, base, leader);
-    return base + (uint32_t)(lane - leader);
+    r.len = (uint32_t)(end - lane);
+    return r;
 }
 
 // keys: cell key of each particle, its slot within the cell (run-aggregated
-// atomics) and the per-chunk totals that the scan needs.
+// atomics) and the per-chunk totals that the scan needs.  Each block takes
+// kKeyTiles consecutive work items, with their loads, then their atomics,
+// then their shuffles issued together.
+constexpr int kKeyTiles = 4;
+
 __global__ void __launch_bounds__(kMaxTile) k_keys(DevArrays a) {
     const int nwork = *a.n_ptiles;
     const int lane = threadIdx.x & 31;
-    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-        const Work wk = a.ptiles[w];
-        if (a.steps_left[wk.scene] == 0) continue;
-        const SceneDev& S = a.scenes[wk.scene];
-        const int i = wk.start + threadIdx.x;
-        const bool valid = i < S.p_off + S.n;
-        const unsigned mask = __ballot_sync(kFull, valid);
-        if (!valid) continue;
-        const float4 x = a.pos[i];
-        const Cell c = cell_of(S, x.x, x.y, x.z);
-        const uint32_t k = row_key(a.tab, S, c.cy, c.cz) + (uint32_t)c.cx;
-        const uint32_t slot = run_aggregated_add(a.counts, (uint32_t)S.k_off + k, mask, lane);
-        a.key[i] = k;
-        a.slot[i] = slot;
-        run_aggregated_add(a.chunk_sum, (uint32_t)S.c_off + (k >> kChunkBits), mask, lane);
+    for (int w0 = blockIdx.x * kKeyTiles; w0 < nwork; w0 += gridDim.x * kKeyTiles) {
+        bool valid[kKeyTiles];
+        int idx[kKeyTiles];
+        uint32_t k[kKeyTiles], gk[kKeyTiles], ck[kKeyTiles];
+        float4 x[kKeyTiles];
+#pragma unroll
+        for (int u = 0; u < kKeyTiles; ++u) {
+            valid[u] = false;
+            idx[u] = 0;
+            const int w = w0 + u;
+            if (w < nwork) {
+                const Work wk = a.ptiles[w];
+                if (a.steps_left[wk.scene] != 0) {
+                    const SceneDev& S = a.scenes[wk.scene];
+                    idx[u] = wk.start + threadIdx.x;
+                    valid[u] = idx[u] < S.p_off + S.n;
+                    if (valid[u]) x[u] = a.pos[idx[u]];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kKeyTiles; ++u) {
+            if (!valid[u]) continue;
+            const SceneDev& S = a.scenes[a.ptiles[w0 + u].scene];
+            const Cell c = cell_of(S, x[u].x, x[u].y, x[u].z);
+            k[u] = row_key(a.tab, S, c.cy, c.cz) + (uint32_t)c.cx;
+            gk[u] = (uint32_t)S.k_off + k[u];
+            ck[u] = (uint32_t)S.c_off + (k[u] >> kChunkBits);
+        }
+        Run rk[kKeyTiles];
+        uint32_t base[kKeyTiles];
+#pragma unroll
+        for (int u = 0; u < kKeyTiles; ++u) {
+            const unsigned mask = __ballot_sync(kFull, valid[u]);
+            base[u] = 0;
+            if (!valid[u]) continue;
+            rk[u] = run_of(gk[u], mask, lane);
+            const Run rc = run_of(ck[u], mask, lane);
+            if (rk[u].start) base[u] = atomicAdd(a.counts + gk[u], rk[u].len);
+            if (rc.start) atomicAdd(a.chunk_sum + ck[u], rc.len);
+        }
+#pragma unroll
+        for (int u = 0; u < kKeyTiles; ++u) {
+            const unsigned mask = __ballot_sync(kFull, valid[u]);
+            if (!valid[u]) continue;
+            const uint32_t b = __shfl_sync(mask, base[u], rk[u].leader);
+            a.key[idx[u]] = k[u];
+            a.slot[idx[u]] = b + (uint32_t)(lane - rk[u].leader);
+        }
     }
 }
 
@@ -635,7 +679,7 @@ __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
 // LISTED: the in-range pairs are compacted (for_each_in_range_listed) instead
 // of evaluated inside the candidate loop; which one is faster depends on the
 // neighbour density, so the autotuner picks it.
-template <bool ORDERED, bool LISTED, int MINB, bool NL = false, bool X2 = false>
+template <bool ORDERED, bool LISTED, int MINB, bool NL = false, bool X2 = false, bool PACK = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
@@ -689,7 +733,13 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
             if (NL) a.ncnt[p] = cnt;
         }
         const float P = fm(S.k, fs(rho, S.p0));
-        a.dyn[p] = make_float4(rho, fdv(P, fm(rho, rho)), fdv(S.mass, rho), P);
+        const float Ai = fdv(P, fm(rho, rho)), Bi = fdv(S.mass, rho);
+        a.dyn[p] = make_float4(rho, Ai, Bi, P);
+        if (PACK) {
+            const float4 vi = a.svel[p];
+            a.fdat[2 * (size_t)p] = make_float4(xi.x, xi.y, xi.z, Ai);
+            a.fdat[2 * (size_t)p + 1] = make_float4(vi.x, vi.y, vi.z, Bi);
+        }
     }
 }
 
@@ -743,7 +793,7 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
                     const uint32_t j = __ldg(nl);
                     pair(j, __ldg(sp + j));
                 }
-            } else {
+            } else if (NL == 2) {
                 const uint32_t* nl = a.nlist + p;
                 const int64_t stride = a.nl_stride;
                 uint32_t j0 = cnt > 0 ? __ldg(nl) : 0u;
@@ -769,6 +819,37 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
                     x0 = x1;
                     v0 = v1;
                     d0 = d1;
+                }
+            } else {
+                // NL == 3: the same walk over the packed 32-byte records (one
+                // sector per neighbour); the id is read only in record mode
+                const uint32_t* nl = a.nlist + p;
+                const int64_t stride = a.nl_stride;
+                const float4* fd = a.fdat + 2 * (size_t)S.p_off;
+                const bool rec = (S.flags & kFlagRecord) != 0;
+                uint32_t j0 = cnt > 0 ? __ldg(nl) : 0u;
+                uint32_t j1 = cnt > 1 ? __ldg(nl + stride) : 0u;
+                float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), b0 = a0;
+                if (cnt > 0) {
+                    a0 = __ldg(fd + 2 * j0);
+                    b0 = __ldg(fd + 2 * j0 + 1);
+                }
+                nl += 2 * stride;
+                for (int q = 0; q < cnt; ++q, nl += stride) {
+                    const uint32_t j2 = (q + 2 < cnt) ? __ldg(nl) : 0u;
+                    float4 a1 = a0, b1 = b0;
+                    if (q + 1 < cnt) {
+                        a1 = __ldg(fd + 2 * j1);
+                        b1 = __ldg(fd + 2 * j1 + 1);
+                    }
+                    const int idj = rec ? __float_as_int(__ldg(&sp[j0].w)) : 0;
+                    const float rx = fs(xi.x, a0.x), ry = fs(xi.y, a0.y), rz = fs(xi.z, a0.z);
+                    force_pair(S, acc, rx, ry, rz, fsq(dist2(rx, ry, rz)), vi.x, vi.y, vi.z, Ai, b0, a0.w, b0.w, idj,
+                               (int)j0 == pl);
+                    j0 = j1;
+                    j1 = j2;
+                    a0 = a1;
+                    b0 = b1;
                 }
             }
             if (!valid) continue;
@@ -944,7 +1025,7 @@ __global__ void __launch_bounds__(256) k_diag(DevArrays a, double* partial, long
 }  // namespace
 
 void launch_keys(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_keys<<<s.grid_p, s.tile, 0, st>>>(a);
+    k_keys<<<(s.grid_p + kKeyTiles - 1) / kKeyTiles, s.tile, 0, st>>>(a);
 }
 void launch_scan(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     k_scan<<<s.grid_c, kScanThreads, 0, st>>>(a);
@@ -1037,6 +1118,8 @@ void configure_kernels() {
     cudaFuncSetAttribute(k_force<false, 3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, 3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.tile * sizeof(uint32_t); }
@@ -1046,18 +1129,31 @@ static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.til
 // Bit 3 hands the in-range neighbour lists from the density pass to the force
 // pass (takes precedence over bit 0); bit 4 with it pipelines the force
 // pass's list walk; bit 5 with it gives the density pass a middle register
-// budget (6 resident blocks of 256 threads).
+// budget (6 resident blocks of 256 threads); bit 6 pairs the density pass's
+// candidate loads; bit 7 with bit 3 packs each particle's force-pass inputs
+// into one 32-byte record.
+template <int MINB>
+static void launch_density_nl(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    const bool x2 = (s.variant & 64) != 0, pack = (s.variant & 128) != 0;
+    if (x2 && pack)
+        k_density<false, false, MINB, true, true, true><<<s.grid_p, s.tile, 0, st>>>(a);
+    else if (x2)
+        k_density<false, false, MINB, true, true, false><<<s.grid_p, s.tile, 0, st>>>(a);
+    else if (pack)
+        k_density<false, false, MINB, true, false, true><<<s.grid_p, s.tile, 0, st>>>(a);
+    else
+        k_density<false, false, MINB, true, false, false><<<s.grid_p, s.tile, 0, st>>>(a);
+}
+
 void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     const bool relaxed = (s.variant & 4) != 0;
     if (s.variant & 8) {
         if (relaxed)
-            k_density<false, false, 4, true><<<s.grid_p, s.tile, 0, st>>>(a);
+            launch_density_nl<4>(a, s, st);
         else if (s.variant & 32)
-            k_density<false, false, 6, true><<<s.grid_p, s.tile, 0, st>>>(a);
-        else if (s.variant & 64)
-            k_density<false, false, 8, true, true><<<s.grid_p, s.tile, 0, st>>>(a);
+            launch_density_nl<6>(a, s, st);
         else
-            k_density<false, false, 8, true><<<s.grid_p, s.tile, 0, st>>>(a);
+            launch_density_nl<8>(a, s, st);
     } else if (s.variant & 1) {
         if (relaxed)
             k_density<false, true, 4><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
@@ -1074,7 +1170,12 @@ void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream
     k_density<true, false, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    if ((s.variant & 24) == 24) {
+    if ((s.variant & 136) == 136) {
+        if (s.variant & 4)
+            k_force<false, 3, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+        else
+            k_force<false, 4, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+    } else if ((s.variant & 24) == 24) {
         if (s.variant & 4)
             k_force<false, 3, 2><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
         else

@@ -46,6 +46,9 @@ struct DevArrays {
     uint32_t* nlist;
     int32_t* ncnt;
     int64_t nl_stride;
+    // packed neighbour records (variant bit 7), two float4 per sorted
+    // particle: (x, y, z, P/rho^2) and (vx, vy, vz, m/rho)
+    float4* fdat;
     // status word: bit 0 = ordered-mode neighbour overflow
     unsigned* status;
 };

@@ -215,11 +215,12 @@ def test_kernel_variants_identical(golden, cell_mult):
     """Every kernel variant visits the in-range neighbours in the same order:
     compacted density lists (1), relaxed registers (4), neighbour lists
     handed from the density to the force pass (8, 12), walked with loads
-    ahead (24, 28, 56), with paired candidate loads (88) give the same bits
-    as the cell traversal in both passes (0), records and NeighbId included."""
+    ahead (24, 28, 56), with paired candidate loads (88) and over packed
+    neighbour records (152, 216) give the same bits as the cell traversal in
+    both passes (0), records and NeighbId included."""
     g = golden("ref_c1_2048.npz")
     base = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=0)
-    for v in (1, 4, 8, 12, 24, 28, 56, 88):
+    for v in (1, 4, 8, 12, 24, 28, 56, 88, 152, 216):
         got = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=v)
         for s in (1, 30):
             assert np.array_equal(got[s][0], base[s][0]), (v, s)
@@ -234,7 +235,7 @@ def test_neighbour_list_overflow_falls_back_exactly():
     lattice = np.stack(np.meshgrid(*[np.arange(-0.18, 0.18, 0.024)] * 3, indexing="ij"), -1).reshape(-1, 3)
     pos = np.concatenate([blob, lattice[np.abs(lattice).max(1) > 0.05]]).astype(np.float32)
     a = run(REF, pos, [1, 5], variant=0)
-    for v in (8, 24, 88):
+    for v in (8, 24, 88, 216):
         b = run(REF, pos, [1, 5], variant=v)
         for s in (1, 5):
             assert np.array_equal(a[s][0], b[s][0]) and np.array_equal(a[s][1], b[s][1])
