@@ -137,7 +137,7 @@ SPH_API int sph_system_destroy(sph_system* s);
 /* Advance every active scene nsteps (FluidSystemSPH::Run, fluid_system.h:104-183,
  * once per step).  Enqueued on the system's stream; returns without waiting. */
 SPH_API int sph_system_step(sph_system* s, int nsteps);
-SPH_API int sph_system_sync(sph_system* s);
+SPH_API int sph_system_sync(sph_system* s);  /* waits for steps and asynchronous readbacks */
 /* Device time of nsteps steps measured with CUDA events on the system stream. */
 SPH_API int sph_system_time_steps(sph_system* s, int nsteps, float* ms);
 /* Device time per stage of one step, averaged over nsteps (stages: keys, scan,
@@ -193,6 +193,17 @@ SPH_API int sph_scene_count(sph_system* s, int scene, int* n);
 /* Positions, velocities, densities and sediment in id order (any may be NULL). */
 SPH_API int sph_scene_get_particles(sph_system* s, int scene, float* pos3, float* vel3, float* density,
                             int32_t* sediment);
+/* The same readback without waiting (no counterpart in the reference: the
+ * front end's per-frame position readback, overlapped with the next steps).
+ * It reads the state after all steps enqueued so far; the buffers are
+ * complete once sph_system_sync returns and must not be touched before.  The
+ * copies overlap later steps only when the buffers are pinned
+ * (sph_host_alloc). */
+SPH_API int sph_scene_get_particles_async(sph_system* s, int scene, float* pos3, float* vel3, float* density,
+                                          int32_t* sediment);
+/* Pinned (page-locked) host memory for the asynchronous readback. */
+SPH_API int sph_host_alloc(int64_t bytes, void** out);
+SPH_API int sph_host_free(void* p);
 /* GetParticle(id) (fluid_system.h:286-289).  Force fields are filled when the
  * scene has SPH_FLAG_RECORD, zero otherwise. */
 SPH_API int sph_scene_get_particle(sph_system* s, int scene, int id, sph_particle* out);

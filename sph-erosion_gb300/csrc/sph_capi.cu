@@ -218,6 +218,26 @@ int sph_scene_get_particles(sph_system* s, int scene, float* pos3, float* vel3, 
     return guard([&] { sys(s).get_particles(scene, pos3, vel3, density, sediment); });
 }
 
+int sph_scene_get_particles_async(sph_system* s, int scene, float* pos3, float* vel3, float* density,
+                                  int32_t* sediment) {
+    return guard([&] { sys(s).get_particles_async(scene, pos3, vel3, density, sediment); });
+}
+
+int sph_host_alloc(int64_t bytes, void** out) {
+    return guard([&] {
+        need(out, "out");
+        *out = nullptr;
+        if (bytes <= 0) throw sph::Error(SPH_ERR_INVALID, "bytes must be positive");
+        sph::check_cuda(cudaMallocHost(out, (size_t)bytes), "cudaMallocHost");
+    });
+}
+
+int sph_host_free(void* p) {
+    return guard([&] {
+        if (p) sph::check_cuda(cudaFreeHost(p), "cudaFreeHost");
+    });
+}
+
 int sph_scene_get_particle(sph_system* s, int scene, int id, sph_particle* out) {
     return guard([&] {
         need(out, "out");

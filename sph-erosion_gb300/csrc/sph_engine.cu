@@ -174,6 +174,11 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
     SPH_CK(cudaSetDevice(dev_));
     SPH_CK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
     SPH_CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    SPH_CK(cudaStreamCreateWithFlags(&cst_, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+        SPH_CK(cudaEventCreateWithFlags(&gathered_[k], cudaEventDisableTiming));
+        SPH_CK(cudaEventCreateWithFlags(&copied_[k], cudaEventDisableTiming));
+    }
     configure_kernels();
     SPH_CK(cudaGetLastError());
     pa_.reset(0);
@@ -199,6 +204,13 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
 System::~System() {
     drop_graph();
     if (st_) cudaStreamSynchronize(st_);
+    if (cst_) cudaStreamSynchronize(cst_);
+    for (int k = 0; k < 2; ++k) {
+        astage_[k].release();
+        if (gathered_[k]) cudaEventDestroy(gathered_[k]);
+        if (copied_[k]) cudaEventDestroy(copied_[k]);
+    }
+    if (cst_) cudaStreamDestroy(cst_);
     DevBuf<float4>* f4[] = {&pos_, &vel_, &spos_, &svel_, &dyn_};
     for (auto* b : f4) b->release();
     key_.release(); slot_.release(); perm_.release();
@@ -457,12 +469,14 @@ void System::fill_dev(Scene& sc) {
     d.layer = p.erosion_layer;
 }
 
+// Stream-ordered: kernels enqueued before see the old descriptor, later ones
+// the new.  The sources are pageable host memory, which the copy stages
+// before returning, so the host may change them right after.
 void System::upload_scene(int id) {
     Scene& sc = scenes_[id];
     fill_dev(sc);
     SPH_CK(cudaMemcpyAsync(dscenes_.p + id, &sc.dev, sizeof(SceneDev), cudaMemcpyHostToDevice, st_));
     SPH_CK(cudaMemcpyAsync(steps_.p + id, &sc.steps, sizeof(int), cudaMemcpyHostToDevice, st_));
-    SPH_CK(cudaStreamSynchronize(st_));
 }
 
 static void validate(const sph_params& p) {
@@ -688,6 +702,41 @@ void System::get_particles(int id, float* pos3, float* vel3, float* density, int
     if (density) SPH_CK(cudaMemcpyAsync(density, d_den, (size_t)n * 4, cudaMemcpyDeviceToHost, st_));
     if (sed) SPH_CK(cudaMemcpyAsync(sed, d_sed, (size_t)n * 4, cudaMemcpyDeviceToHost, st_));
     SPH_CK(cudaStreamSynchronize(st_));
+}
+
+// The same readback without waiting: the gather into id order runs on the
+// library stream after the work already enqueued (so it sees the state of the
+// last step), the copies into the caller's buffers on a second stream, so
+// that they overlap the steps enqueued next.  Two staging buffers alternate;
+// a gather waits for the copies that last used its buffer.  The caller's
+// buffers are complete after sph_system_sync; with pageable buffers the
+// copies cannot overlap anything (the driver completes them before
+// returning), so the caller should pass pinned memory.
+void System::get_particles_async(int id, float* pos3, float* vel3, float* density, int32_t* sed) {
+    Scene& sc = scene(id);
+    const int n = sc.n;
+    if (n == 0) return;
+    const int k = aslot_;
+    aslot_ ^= 1;
+    if (astage_[k].n < (int64_t)8 * n) {
+        SPH_CK(cudaStreamSynchronize(cst_));
+        astage_[k].resize((int64_t)8 * n, false, st_);
+    }
+    SPH_CK(cudaStreamWaitEvent(st_, copied_[k], 0));
+    float* d_pos = astage_[k].p;
+    float* d_vel = astage_[k].p + (size_t)3 * n;
+    float* d_den = astage_[k].p + (size_t)6 * n;
+    int32_t* d_sed = reinterpret_cast<int32_t*>(astage_[k].p + (size_t)7 * n);
+    launch_gather_by_id(pos_.p, vel_.p, dyn_.p, (int)sc.p_off, n, pos3 ? d_pos : nullptr, vel3 ? d_vel : nullptr,
+                        density ? d_den : nullptr, sed ? d_sed : nullptr, st_);
+    SPH_CK(cudaGetLastError());
+    SPH_CK(cudaEventRecord(gathered_[k], st_));
+    SPH_CK(cudaStreamWaitEvent(cst_, gathered_[k], 0));
+    if (pos3) SPH_CK(cudaMemcpyAsync(pos3, d_pos, (size_t)n * 12, cudaMemcpyDeviceToHost, cst_));
+    if (vel3) SPH_CK(cudaMemcpyAsync(vel3, d_vel, (size_t)n * 12, cudaMemcpyDeviceToHost, cst_));
+    if (density) SPH_CK(cudaMemcpyAsync(density, d_den, (size_t)n * 4, cudaMemcpyDeviceToHost, cst_));
+    if (sed) SPH_CK(cudaMemcpyAsync(sed, d_sed, (size_t)n * 4, cudaMemcpyDeviceToHost, cst_));
+    SPH_CK(cudaEventRecord(copied_[k], cst_));
 }
 
 void System::get_records(int id, float* rec27, int* nbid, int32_t* sed) {
@@ -1017,6 +1066,7 @@ void System::advance_step_mirror(int nsteps) {
 
 void System::sync() {
     SPH_CK(cudaStreamSynchronize(st_));
+    SPH_CK(cudaStreamSynchronize(cst_));
     check_status();
 }
 

@@ -82,6 +82,7 @@ class System {
     int add_lattice(int id, int n, const float origin[3]);
     int count(int id) const { return scene(id).n; }
     void get_particles(int id, float* pos3, float* vel3, float* density, int32_t* sed);
+    void get_particles_async(int id, float* pos3, float* vel3, float* density, int32_t* sed);
     void get_records(int id, float* rec27, int* nbid, int32_t* sed);
     void diag(int id, sph_diag* out);
     void set_terrain(int id, int w, int d, const float* heights);
@@ -138,6 +139,12 @@ class System {
     void upload_terrain_height(Scene& sc);
 
     sph_system_config cfg_;
+    // asynchronous readback: gathers on st_ into one of two staging buffers,
+    // device-to-host copies on cst_
+    cudaStream_t cst_ = nullptr;
+    cudaEvent_t gathered_[2] = {nullptr, nullptr}, copied_[2] = {nullptr, nullptr};
+    DevBuf<float> astage_[2];
+    int aslot_ = 0;
     int dev_ = 0, nsm_ = 1;
     cudaStream_t st_ = nullptr;
     std::vector<Scene> scenes_;

@@ -153,6 +153,10 @@ SIGNATURES = {
     "sph_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "sph_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sph_server_run_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(ServerStats)]),
+    "sph_scene_get_particles_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p]),
+    "sph_host_alloc": (C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
+    "sph_host_free": (C.c_int, [C.c_void_p]),
     "sph_grid_collision_u8": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p]),
 }
@@ -249,6 +253,18 @@ def _ck(rc: int):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def pinned_empty(shape, dtype=np.float32):
+    """A numpy array in pinned host memory (freed with the array)."""
+    import weakref
+
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    ptr = C.c_void_p()
+    _ck(lib().sph_host_alloc(max(n, 1), C.byref(ptr)))
+    buf = (C.c_byte * max(n, 1)).from_address(ptr.value)
+    weakref.finalize(buf, lib().sph_host_free, ptr.value)
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
 
 def grid_collision(hmap, dims, cur, nxt, vel):
@@ -425,6 +441,12 @@ class Scene:
         n = self.count()
         out = np.zeros((n, 3), np.float32) if out is None else out
         _ck(lib().sph_scene_get_particles(self.h, self.id, _p(out), None, None, None))
+        return out
+
+    def get_positions_async(self, out):
+        """Enqueue the positions readback into `out` (pinned, see
+        pinned_empty); complete after System.sync()."""
+        _ck(lib().sph_scene_get_particles_async(self.h, self.id, _p(out), None, None, None))
         return out
 
     def get_records(self):

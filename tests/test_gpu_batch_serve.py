@@ -145,3 +145,22 @@ def test_server_submit_poll():
                 break
         assert sorted(r.ticket for r in got) == sorted(tickets)
         assert all(r.total_units == 0 for r in got)
+
+
+def test_async_readback_matches_sync():
+    """Positions read without waiting (into pinned buffers, copies on the
+    second stream) equal the synchronous readback after the same steps."""
+    req = dict(seed=31, particles=5000, terrain_side=64, steps=0)
+    with S.System() as sysm:
+        sc = sysm.scene_from_request(W.base_params(), req)
+        n = sc.count()
+        bufs = [S.pinned_empty((n, 3)) for _ in range(4)]
+        for b in bufs:
+            sysm.step(3)
+            sc.get_positions_async(b)
+        sysm.sync()
+    with S.System() as ref:
+        rs = ref.scene_from_request(W.base_params(), req)
+        for b in bufs:
+            ref.step(3)
+            assert np.array_equal(b, rs.get_positions())
