@@ -683,6 +683,7 @@ int System::add_lattice(int id, int n, const float origin[3]) {
 }
 
 void System::get_particles(int id, float* pos3, float* vel3, float* density, int32_t* sed) {
+    Range r("sph/readback");
     Scene& sc = scene(id);
     SPH_CK(cudaStreamSynchronize(st_));
     check_status();
@@ -713,6 +714,7 @@ void System::get_particles(int id, float* pos3, float* vel3, float* density, int
 // copies cannot overlap anything (the driver completes them before
 // returning), so the caller should pass pinned memory.
 void System::get_particles_async(int id, float* pos3, float* vel3, float* density, int32_t* sed) {
+    Range r("sph/readback_async");
     Scene& sc = scene(id);
     const int n = sc.n;
     if (n == 0) return;
@@ -1003,27 +1005,40 @@ void System::enqueue_step(const DevArrays& a, const LaunchShape& s, cudaEvent_t*
         if (ev) SPH_CK(cudaEventRecord(ev[i], st_));
     };
     mark(0);
-    launch_keys(a, s, st_);
-    mark(1);
-    launch_scan(a, s, st_);
-    mark(2);
-    launch_scatter(a, s, st_);
-    mark(3);
-    launch_reorder(a, s, st_);
-    mark(4);
-    if (any_fast_) launch_density(a, s, st_);
-    if (any_ordered_) launch_density_ordered(a, s, st_);
-    mark(5);
-    if (any_fast_) launch_force(a, s, st_);
-    if (any_ordered_) launch_force_ordered(a, s, st_);
-    mark(6);
-    if (any_terrain_ && s.grid_t > 0) launch_terrain(a, s, st_);
-    mark(7);
-    if (any_limited_) launch_tick(a, (int)scenes_.size(), st_);
-    mark(8);
+    {
+        Range r("sph/sort");
+        launch_keys(a, s, st_);
+        mark(1);
+        launch_scan(a, s, st_);
+        mark(2);
+        launch_scatter(a, s, st_);
+        mark(3);
+        launch_reorder(a, s, st_);
+        mark(4);
+    }
+    {
+        Range r("sph/density");
+        if (any_fast_) launch_density(a, s, st_);
+        if (any_ordered_) launch_density_ordered(a, s, st_);
+        mark(5);
+    }
+    {
+        Range r("sph/force");
+        if (any_fast_) launch_force(a, s, st_);
+        if (any_ordered_) launch_force_ordered(a, s, st_);
+        mark(6);
+    }
+    {
+        Range r("sph/terrain");
+        if (any_terrain_ && s.grid_t > 0) launch_terrain(a, s, st_);
+        mark(7);
+        if (any_limited_) launch_tick(a, (int)scenes_.size(), st_);
+        mark(8);
+    }
 }
 
 void System::capture_graph() {
+    Range r("sph/capture_graph");
     drop_graph();
     const DevArrays a = arrays();
     const LaunchShape s = shape();
@@ -1037,6 +1052,7 @@ void System::capture_graph() {
 }
 
 void System::step(int nsteps) {
+    Range r("sph/step");
     if (nsteps < 0) throw Error(SPH_ERR_INVALID, "negative step count");
     if (work_dirty_) rebuild_work();
     if (n_ptiles_ > 0 && nsteps > 0) {
@@ -1186,6 +1202,7 @@ void System::neighbour_counts(int id, int32_t* out) {
 
 // ---- autotuner ------------------------------------------------------------------
 void System::autotune(int steps, sph_tune_result* out) {
+    Range r("sph/autotune");
     if (steps <= 0) throw Error(SPH_ERR_INVALID, "autotune needs steps > 0");
     std::memset(out, 0, sizeof *out);
     if (work_dirty_) rebuild_work();

@@ -14,7 +14,18 @@
 #include "sph_kernels.h"
 #include "sph_types.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace sph {
+
+// NVTX range for profilers (ncu --nvtx): stage names of the step, autotuner,
+// readbacks and server rounds.  Costs a pointer test without a tool attached.
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 
 struct Error : std::runtime_error {
     int code;

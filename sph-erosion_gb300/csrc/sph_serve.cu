@@ -138,6 +138,7 @@ class Server {
     }
 
     void admit() {
+        Range rg("sph/serve_admit");
         const double t = now();
         while (!queue_.empty() && queue_.front().arrival <= t) {
             const Pending& q = queue_.front();
@@ -170,6 +171,7 @@ class Server {
     }
 
     void retire() {
+        Range rg("sph/serve_retire");
         const double t = now();
         std::vector<Active> keep;
         for (Active& a : active_) {

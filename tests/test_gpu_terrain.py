@@ -93,3 +93,23 @@ def test_grid_collision_edges(golden):
         S.grid_collision(hm, (100, 513), cur, nxt, nxt - cur)
     with pytest.raises(ValueError):
         S.grid_collision(hm[:100], (100, 100), cur, nxt, nxt - cur)
+
+
+def test_grid_collision_known_answers():
+    """Known answers derived from grid.h (and confirmed with the reference's
+    own code): a particle moving down through a flat field at height H lands
+    on y = H with the normal (0, 1, 0); one that stops above it has no
+    contact; on the terraced field 10 + x/8 the contact is on the terrace."""
+    flat = np.full((512, 512), 10, np.uint8)
+    cur = np.array([[30.25, 12.0, 40.5], [30.25, 12.0, 40.5]], np.float32)
+    nxt = np.array([[30.3, 9.5, 40.55], [30.3, 10.5, 40.55]], np.float32)
+    hit, cp, nr = S.grid_collision(flat, (100, 256, 100), cur, nxt, (nxt - cur) / 0.01)
+    assert hit.tolist() == [True, False]
+    assert np.array_equal(cp[0], np.float32([30.3, 10.0, 40.55])) and np.array_equal(nr[0], [0, 1, 0])
+    assert not cp[1].any() and not nr[1].any()
+    x = np.arange(512)[:, None] * np.ones((1, 512))
+    terraced = (10 + x // 8).astype(np.uint8)
+    cur = np.array([[20.3, 13.5, 20.6]], np.float32)
+    nxt = np.array([[20.35, 11.0, 20.62]], np.float32)
+    hit, cp, nr = S.grid_collision(terraced, (100, 256, 100), cur, nxt, (nxt - cur) / 0.01)
+    assert hit[0] and np.array_equal(cp[0], np.float32([20.35, 12.0, 20.62])) and np.array_equal(nr[0], [0, 1, 0])
