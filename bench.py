@@ -20,6 +20,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -170,6 +171,13 @@ def traversal(scene, step_ms):
             "reference_pair_tests_per_step": 3 * n * n}
 
 
+SPINUP = {"plain_1m": 1000, "plain_small": 500, "skew": 2000, "batched": 500}
+
+
+def spinup_steps(args):
+    return SPINUP.get(args.workload, 0) if args.spinup is None else args.spinup
+
+
 def flush_l2(buf):
     buf.zero_()
 
@@ -192,8 +200,14 @@ def run_ours(args, spec, config):
     spec = dict(spec, params=dict(spec["params"], cell_mult=args.cell_mult))
     sc = W.build_scene(sysm, spec)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    # warm-up, then the autotuner picks tile and cell size from this state
-    # (each trial restarts from a snapshot; the state is restored after)
+    # spin-up to the middle of the configured run (untimed: the flow has
+    # collapsed and compressed by then, which is what most of the run's steps
+    # look like), warm-up, then the autotuner picks tile, cell size and
+    # variant from this state (each trial restarts from a snapshot; the
+    # state is restored after)
+    spin = spinup_steps(args)
+    if spin:
+        sysm.step(spin)
     for _ in range(args.warmup):
         sysm.step(1)
     sysm.sync()
@@ -334,8 +348,17 @@ def run_batched(args, config):
     base = W.base_params(args.cell_mult)
     sysm = S.System(particle_capacity=total + 512 * len(reqs), key_capacity=1 << 24, terrain_capacity=1 << 24,
                     tile=args.tile, graph_steps=16, device=local, variant=args.variant)
-    for r in reqs:
-        sysm.scene_from_request(base, r)
+    scenes = [sysm.scene_from_request(base, r) for r in reqs]
+    # spin-up (untimed), then each scene's state is checkpointed so that the
+    # plain form starts every scene from the same state
+    spin = spinup_steps(args)
+    tmp = tempfile.mkdtemp(prefix="sph_bench_")
+    if spin:
+        sysm.step(spin)
+    paths = []
+    for k, sc in enumerate(scenes):
+        paths.append(os.path.join(tmp, f"scene{k}.sphe"))
+        sc.save(paths[-1])
     sysm.step(args.warmup)
     sysm.sync()
     tuned = sysm.autotune(4) if args.autotune else None
@@ -348,10 +371,12 @@ def run_batched(args, config):
     cm = tuned["cell_mult"] if tuned else args.cell_mult
     variant = tuned["variant"] if tuned else args.variant
     plain_ms = 0.0
-    for r in reqs:
+    for r, path in zip(reqs, paths):
         with S.System(particle_capacity=r["particles"], tile=tile, graph_steps=16, device=local,
                       variant=variant) as one:
-            one.scene_from_request(W.base_params(cm), r)
+            sc1 = one.scene_from_request(W.base_params(cm), r)
+            sc1.load(path)
+            os.remove(path)
             one.step(args.warmup)
             one.sync()
             plain_ms += one.time_steps(args.steps)
@@ -390,7 +415,8 @@ def run_serving(args, config):
     lat = [r.done_s - r.arrival_s for r in res]
     bad = sum(1 for r in res if r.total_units != 0 or r.nan_particles != 0)
     parts = _gather(dict(lat=lat, bad=bad, ps=st["particle_steps"], wall=st["wall_s"], peak=st["peak_active"],
-                         peak_p=st["peak_particles"], peak_b=st["peak_bytes"], chunks=st["chunks"]), ws)
+                         peak_p=st["peak_particles"], peak_b=st["peak_bytes"], chunks=st["chunks"],
+                         phases={k: st[k] for k in ("admit_s", "prepare_s", "gpu_wait_s", "retire_s")}), ws)
     if rank != 0:
         return
     lat = np.sort(np.concatenate([np.asarray(q["lat"]) for q in parts]))
@@ -410,6 +436,7 @@ def run_serving(args, config):
             "wall_s": wall, "peak_active": max(q["peak"] for q in parts),
             "peak_particles": max(q["peak_p"] for q in parts), "peak_bytes": max(q["peak_b"] for q in parts),
             "chunks": sum(q["chunks"] for q in parts), "mass_violations": sum(q["bad"] for q in parts),
+            "host_phases_s": parts[0]["phases"],
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -433,6 +460,9 @@ def main():
     ap.add_argument("--requests", type=int, default=400, help="serving: requests in the trace")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
     ap.add_argument("--particles", type=int, default=8388608, help="skew: particles (the box floor scales with them)")
+    ap.add_argument("--spinup", type=int, default=None,
+                    help="untimed steps before the warm-up (default: to mid-run; plain_1m 1000 of its 2000 steps, "
+                         "skew 2000, batched 500, plain_small 500)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="warm-up and timed steps only (for profiler captures); prints nothing")
     args = ap.parse_args()
@@ -440,6 +470,9 @@ def main():
 
     if args.workload in ("batched", "serving") and args.impl == "ours":
         cfg = {"h": W.H, "dt": W.PHYS["dt"], "erosion": True, "tile": args.tile, "cell_mult": args.cell_mult}
+        if args.workload == "batched":
+            cfg["window"] = (f"steps {spinup_steps(args) + args.warmup + 1}..{spinup_steps(args) + args.warmup + args.steps}"
+                             f" after {spinup_steps(args)} untimed spin-up steps")
         (run_batched if args.workload == "batched" else run_serving)(args, cfg)
         return
     spec = {"plain_small": W.plain_small, "skew": lambda: W.skew_rain(args.particles)}.get(args.workload, W.plain_1m)()
@@ -448,7 +481,9 @@ def main():
               "terrain": f"{t['w']}x{t['d']} fBm {t['octaves']} oct amp {t['amplitude']}" if t else None,
               "box": "x".join(str(2 * b) for b in spec["params"]["box_half"]), "h": spec["params"]["smoothing_radius"],
               "dt": spec["params"]["dt"], "erosion": bool(spec["params"]["erosion"]), "resort": "every step",
-              "l2": "flushed (512 MiB write) before every timed step"}
+              "l2": "flushed (512 MiB write) before every timed step",
+              "window": f"steps {spinup_steps(args) + args.warmup + 1}..{spinup_steps(args) + args.warmup + args.steps} "
+                        f"after {spinup_steps(args)} untimed spin-up steps"}
     if args.impl == "reference":
         run_reference(args, spec, config)
     else:

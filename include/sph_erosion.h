@@ -111,7 +111,7 @@ typedef struct sph_system_config {
                                  1 = density pass over compacted neighbour lists,
                                  4 = relaxed register budget (fewer resident blocks),
                                  8 = the density pass writes each particle's in-range
-                                     neighbours (64 slots, 260 B per particle) and the
+                                     neighbours (128 slots, 516 B per particle) and the
                                      force pass reads them instead of re-testing the
                                      cells; ignored when the HBM budget has no room,
                                 16 = with 8: the force pass's list walk loads ahead,
@@ -335,6 +335,10 @@ typedef struct sph_server_stats {
     int32_t peak_active;     /* most scenes resident at once */
     int32_t chunks;          /* batched launch sequences run */
     int64_t peak_particles;  /* most particles resident at once */
+    /* host wall time by phase of the serving loop (seconds): admission
+     * (scene uploads), preparing queued requests' inputs while a chunk runs
+     * on the GPU, waiting for the chunk, retirement (readback, checks) */
+    double admit_s, prepare_s, gpu_wait_s, retire_s;
 } sph_server_stats;
 
 SPH_API void sph_server_config_default(sph_server_config* c);

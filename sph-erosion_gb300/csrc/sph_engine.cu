@@ -970,7 +970,6 @@ DevArrays System::arrays() const {
     a.rec = rec_.p;
     a.nlist = nlist_.p;
     a.ncnt = ncnt_.p;
-    a.nl_stride = pos_.n;
     a.fdat = fdat_.p;
     a.counts = counts_.p;
     a.offsets = offsets_.p;
@@ -989,7 +988,7 @@ LaunchShape System::shape() const {
     s.grid_p = n_ptiles_;
     s.grid_c = n_ctiles_;
     s.grid_t = n_ttiles_;
-    s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~248);
+    s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~504);
     return s;
 }
 

@@ -202,7 +202,7 @@ class System {
 
 // Host implementation of the seeded fBm generator (sph_terrain.cpp).
 void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, float lacunarity, float gain,
-                 int kind, float* out);
+                 int kind, float* out, int max_threads = 0);
 
 // Sets the calling thread's sph_last_error() message (sph_capi.cu).
 void set_last_error(const std::string& msg);

@@ -710,26 +710,23 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
         } else {
             // NL: the in-range candidates, in visiting order, also go to the
             // particle's neighbour list for the force pass
-            uint32_t* nl = a.nlist + p;
-            const int64_t stride = a.nl_stride;
+            uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
             int cnt = 0;
             auto visit = [&](uint32_t j, float4 xj) {
                 const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
                 if (s <= S.smax) {
                     rho = fa(rho, density_term(S, fsq(s)));
                     if (NL) {
-                        if (cnt < kNbCap) {
-                            *nl = j;
-                            nl += stride;
-                        }
+                        if (cnt < kNbCap) nl[(size_t)cnt * blockDim.x] = j;
                         ++cnt;
                     }
                 }
             };
-            if (X2)
+            if (X2) {
                 for_each_candidate_x2(a, S, xi, visit);
-            else
+            } else {
                 for_each_candidate(a, S, xi, visit);
+            }
             if (NL) a.ncnt[p] = cnt;
         }
         const float P = fm(S.k, fs(rho, S.p0));
@@ -746,8 +743,8 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
 // force: passes 2 and 3 (fluid_system.h:127-178) and advance (:306-353) with
 // the terrain contact, the box collision and the erosion exchange.
 // NL: the in-range neighbours come from the lists the density pass wrote
-// (same order as the traversal, so the same sums); a warp with a particle
-// whose list overflowed traverses the cells as without lists.  NL = 2
+// (same order as the traversal, so the same sums); a particle whose list
+// overflowed walks its cells instead.  NL = 2
 // software-pipelines the list walk: list entries two ahead and the
 // neighbour's state one ahead are loaded before the current pair is summed.
 template <bool ORDERED, int MINB, int NL = 0>
@@ -784,18 +781,22 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
             if (!for_each_in_range_ordered(a, S, xi, pair)) atomicOr(a.status, 1u);
         } else {
             const int cnt = (NL && valid) ? a.ncnt[p] : 0;
-            if (!NL || __any_sync(kFull, cnt > kNbCap)) {
+            if (!NL) {
                 for_each_in_range_listed(a, S, valid, xi, list, [&](uint32_t j) { pair(j, __ldg(sp + j)); });
+            } else if (cnt > kNbCap) {
+                // the list overflowed: this lane walks its cells (same order)
+                for_each_candidate(a, S, xi, [&](uint32_t j, float4 xj) {
+                    if (dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z)) <= S.smax) pair(j, xj);
+                });
             } else if (NL == 1) {
-                const uint32_t* nl = a.nlist + p;
-                const int64_t stride = a.nl_stride;
-                for (int q = 0; q < cnt; ++q, nl += stride) {
-                    const uint32_t j = __ldg(nl);
+                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
+                for (int q = 0; q < cnt; ++q) {
+                    const uint32_t j = __ldg(nl + (size_t)q * blockDim.x);
                     pair(j, __ldg(sp + j));
                 }
             } else if (NL == 2) {
-                const uint32_t* nl = a.nlist + p;
-                const int64_t stride = a.nl_stride;
+                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
+                const int stride = blockDim.x;
                 uint32_t j0 = cnt > 0 ? __ldg(nl) : 0u;
                 uint32_t j1 = cnt > 1 ? __ldg(nl + stride) : 0u;
                 float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), v0 = x0, d0 = x0;
@@ -823,8 +824,8 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
             } else {
                 // NL == 3: the same walk over the packed 32-byte records (one
                 // sector per neighbour); the id is read only in record mode
-                const uint32_t* nl = a.nlist + p;
-                const int64_t stride = a.nl_stride;
+                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
+                const int stride = blockDim.x;
                 const float4* fd = a.fdat + 2 * (size_t)S.p_off;
                 const bool rec = (S.flags & kFlagRecord) != 0;
                 uint32_t j0 = cnt > 0 ? __ldg(nl) : 0u;
@@ -1114,12 +1115,6 @@ void configure_kernels() {
     cudaFuncSetAttribute(k_density<false, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, 3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.tile * sizeof(uint32_t); }
@@ -1170,21 +1165,23 @@ void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream
     k_density<true, false, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    // the list variants walk their lists (or, on overflow, the cells) per
+    // lane and need no shared memory
     if ((s.variant & 136) == 136) {
         if (s.variant & 4)
-            k_force<false, 3, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 3, 3><<<s.grid_p, s.tile, 0, st>>>(a);
         else
-            k_force<false, 4, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 4, 3><<<s.grid_p, s.tile, 0, st>>>(a);
     } else if ((s.variant & 24) == 24) {
         if (s.variant & 4)
-            k_force<false, 3, 2><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 3, 2><<<s.grid_p, s.tile, 0, st>>>(a);
         else
-            k_force<false, 4, 2><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 4, 2><<<s.grid_p, s.tile, 0, st>>>(a);
     } else if (s.variant & 8) {
         if (s.variant & 4)
-            k_force<false, 3, 1><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 3, 1><<<s.grid_p, s.tile, 0, st>>>(a);
         else
-            k_force<false, 4, 1><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
+            k_force<false, 4, 1><<<s.grid_p, s.tile, 0, st>>>(a);
     } else if (s.variant & 4)
         k_force<false, 3><<<s.grid_p, s.tile, list_bytes(s), st>>>(a);
     else

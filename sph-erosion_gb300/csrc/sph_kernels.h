@@ -40,12 +40,14 @@ struct DevArrays {
     long long* tdelta;
     float* theight;
     // in-range neighbour lists written by the density pass and read by the
-    // force pass (variant bit 3): slot q of sorted particle p at
-    // nlist[q * nl_stride + p], in traversal order; ncnt[p] = in-range count
-    // (may exceed kNbCap: the force pass then traverses the cells again)
+    // force pass (variant bit 3), in traversal order.  Each work tile of T
+    // particles starting at sorted index t owns kNbCap * T entries from
+    // t * kNbCap on, slot-major: entry q of the tile's lane l at q * T + l,
+    // so lanes at the same slot touch consecutive words and a tile's list
+    // stays in one compact region.  ncnt[p] = in-range count (may exceed
+    // kNbCap: that particle's force pass then walks the cells).
     uint32_t* nlist;
     int32_t* ncnt;
-    int64_t nl_stride;
     // packed neighbour records (variant bit 7), two float4 per sorted
     // particle: (x, y, z, P/rho^2) and (vx, vy, vz, m/rho)
     float4* fdat;
@@ -54,7 +56,7 @@ struct DevArrays {
 };
 
 // Slots per particle of the in-range neighbour lists.
-constexpr int kNbCap = 64;
+constexpr int kNbCap = 128;
 
 struct LaunchShape {
     int tile;        // threads per particle tile

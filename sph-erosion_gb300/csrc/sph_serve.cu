@@ -11,6 +11,7 @@
 #include <chrono>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -36,25 +37,42 @@ uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
 
 }  // namespace
 
-// Builds the scene of a request in `sys`; returns its id.
-int scene_from_request(System& sys, const sph_params& base, const sph_request& r) {
+// Host-side inputs of a request's scene: parameters, particles, terrain.
+struct PreparedScene {
+    sph_params p;
+    int particles = 0, side = 0;
+    std::vector<float> pos, hgt;
+};
+
+static PreparedScene prepare_scene(const sph_params& base, const sph_request& r, int fbm_threads) {
+    PreparedScene ps;
     RecipeGeometry g;
     recipe_geometry(r, base.smoothing_radius, &g);
-    sph_params p;
-    recipe_params(base, g, &p);
-    std::vector<float> pos((size_t)r.particles * 3);
-    recipe_particles(r, g, pos.data());
-    std::vector<float> hgt((size_t)r.terrain_side * r.terrain_side);
-    fbm_heights(r.seed, r.terrain_side, r.terrain_side, 6, g.amplitude, 2.0f, 0.5f, 0, hgt.data());
-    const int id = sys.create_scene(p, r.particles, r.terrain_side, r.terrain_side);
+    recipe_params(base, g, &ps.p);
+    ps.particles = r.particles;
+    ps.side = r.terrain_side;
+    ps.pos.resize((size_t)r.particles * 3);
+    recipe_particles(r, g, ps.pos.data());
+    ps.hgt.resize((size_t)r.terrain_side * r.terrain_side);
+    fbm_heights(r.seed, r.terrain_side, r.terrain_side, 6, g.amplitude, 2.0f, 0.5f, 0, ps.hgt.data(), fbm_threads);
+    return ps;
+}
+
+static int create_prepared(System& sys, const PreparedScene& ps) {
+    const int id = sys.create_scene(ps.p, ps.particles, ps.side, ps.side);
     try {
-        sys.set_terrain(id, r.terrain_side, r.terrain_side, hgt.data());
-        sys.set_particles(id, r.particles, pos.data(), nullptr);
+        sys.set_terrain(id, ps.side, ps.side, ps.hgt.data());
+        sys.set_particles(id, ps.particles, ps.pos.data(), nullptr);
     } catch (...) {
         sys.destroy_scene(id);
         throw;
     }
     return id;
+}
+
+// Builds the scene of a request in `sys`; returns its id.
+int scene_from_request(System& sys, const sph_params& base, const sph_request& r) {
+    return create_prepared(sys, prepare_scene(base, r, 0));
 }
 
 class Server {
@@ -73,20 +91,34 @@ class Server {
         if (r.particles <= 0 || r.steps < 0) throw Error(SPH_ERR_INVALID, "request needs particles > 0 and steps >= 0");
         RecipeGeometry g;
         recipe_geometry(r, cfg_.base.smoothing_radius, &g);  // validates early
-        Pending q{next_ticket_++, r, arrival};
+        Pending q{next_ticket_++, r, arrival, nullptr, 0};
         queue_.push_back(q);
         return q.ticket;
     }
 
     // One admission + chunk + retirement round.  Returns the number of
     // requests still queued or resident.
+    // The chunk's steps run on the GPU while the host prepares the inputs of
+    // requests that have arrived and are not yet admitted, so that the next
+    // admission only uploads.
     int poll() {
+        auto t = Clock::now();
+        auto lap = [&](double* acc) {
+            const auto u = Clock::now();
+            *acc += std::chrono::duration<double>(u - t).count();
+            t = u;
+        };
         admit();
+        lap(&stats_.admit_s);
         if (!active_.empty()) {
             sys_.step(cfg_.chunk_steps);
+            prepare_ahead();
+            lap(&stats_.prepare_s);
             sys_.sync();
+            lap(&stats_.gpu_wait_s);
             ++chunks_;
             retire();
+            lap(&stats_.retire_s);
         }
         return (int)(queue_.size() + active_.size());
     }
@@ -106,6 +138,8 @@ class Server {
         int64_t ticket;
         sph_request req;
         double arrival;
+        std::shared_ptr<PreparedScene> prep;  // filled ahead of admission
+        int64_t held = 0;                     // host bytes of prep counted in prepared_bytes_
     };
     struct Active {
         Pending p;
@@ -141,7 +175,7 @@ class Server {
         Range rg("sph/serve_admit");
         const double t = now();
         while (!queue_.empty() && queue_.front().arrival <= t) {
-            const Pending& q = queue_.front();
+            Pending& q = queue_.front();
             const int64_t need = request_bytes(q.req);
             if (need > cfg_.hbm_budget) throw Error(SPH_ERR_CAPACITY, "a request exceeds the whole HBM budget");
             if (reserved_ + need > cfg_.hbm_budget) break;
@@ -150,7 +184,8 @@ class Server {
                 break;
             int id;
             try {
-                id = scene_from_request(sys_, cfg_.base, q.req);
+                if (!q.prep) q.prep = std::make_shared<PreparedScene>(prepare_scene(cfg_.base, q.req, 0));
+                id = create_prepared(sys_, *q.prep);
             } catch (const Error& e) {
                 if (e.code == SPH_ERR_CAPACITY || e.code == SPH_ERR_NOMEM) {
                     if (active_.empty()) throw;
@@ -159,7 +194,8 @@ class Server {
                 throw;
             }
             sys_.set_steps(id, q.req.steps);
-            active_.push_back(Active{q, id, now(), need});
+            prepared_bytes_ -= q.held;
+            active_.push_back(Active{Pending{q.ticket, q.req, q.arrival, nullptr, 0}, id, now(), need});
             reserved_ += need;
             resident_particles_ += q.req.particles;
             queue_.pop_front();
@@ -167,6 +203,50 @@ class Server {
             stats_.peak_particles = std::max<int64_t>(stats_.peak_particles, resident_particles_);
             stats_.peak_bytes = std::max<int64_t>(stats_.peak_bytes, sys_.memory_bytes());
             if (q.req.steps == 0) break;  // retire it on the next round
+        }
+    }
+
+    static int64_t prep_bytes(const Pending& q) {
+        return q.prep ? (int64_t)(q.prep->pos.size() + q.prep->hgt.size()) * 4 : 0;
+    }
+
+    // Prepare, on host threads, the inputs of queued requests that have
+    // arrived, in arrival order, up to kPrepareAhead requests or
+    // kPrepareBytes of host memory held by prepared inputs.
+    static constexpr int kPrepareAhead = 256;
+    static constexpr int64_t kPrepareBytes = (int64_t)1 << 30;
+    void prepare_ahead() {
+        const double t = now();
+        std::vector<Pending*> todo;
+        int64_t bytes = prepared_bytes_;
+        int held = 0;
+        for (Pending& q : queue_) {
+            if (q.arrival > t || held >= kPrepareAhead || bytes >= kPrepareBytes) break;
+            ++held;
+            if (q.prep) continue;
+            todo.push_back(&q);
+            bytes += ((int64_t)q.req.particles * 3 + (int64_t)q.req.terrain_side * q.req.terrain_side) * 4;
+        }
+        if (todo.empty()) return;
+        unsigned nt = std::thread::hardware_concurrency();
+        nt = std::max(1u, std::min<unsigned>(nt ? nt : 1, (unsigned)todo.size()));
+        std::vector<std::shared_ptr<PreparedScene>> out(todo.size());
+        std::vector<std::thread> th;
+        for (unsigned w = 0; w < nt; ++w)
+            th.emplace_back([&, w] {
+                for (size_t k = w; k < todo.size(); k += nt) {
+                    try {
+                        out[k] = std::make_shared<PreparedScene>(prepare_scene(cfg_.base, todo[k]->req, 1));
+                    } catch (...) {
+                        out[k] = nullptr;  // prepared again (and its error raised) at admission
+                    }
+                }
+            });
+        for (auto& x : th) x.join();
+        for (size_t k = 0; k < todo.size(); ++k) {
+            todo[k]->prep = out[k];
+            todo[k]->held = prep_bytes(*todo[k]);
+            prepared_bytes_ += todo[k]->held;
         }
     }
 
@@ -222,6 +302,7 @@ class Server {
     int64_t next_ticket_ = 1;
     int64_t reserved_ = 0;
     int64_t resident_particles_ = 0;
+    int64_t prepared_bytes_ = 0;
     int chunks_ = 0;
     sph_server_stats stats_{};
 

@@ -48,7 +48,7 @@ double noise2(uint64_t oseed, double x, double z) {
 }  // namespace
 
 void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, float lacunarity, float gain, int kind,
-                 float* out) {
+                 float* out, int max_threads) {
     std::vector<uint64_t> oseed(octaves > 0 ? octaves : 1);
     double norm = 0.0, amp = 1.0;
     for (int o = 0; o < octaves; ++o) {
@@ -79,6 +79,7 @@ void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, floa
     const int64_t work = (int64_t)w * d * (octaves > 0 ? octaves : 1);
     unsigned nt = std::thread::hardware_concurrency();
     if (nt == 0) nt = 1;
+    if (max_threads > 0 && nt > (unsigned)max_threads) nt = (unsigned)max_threads;
     if (work < (1 << 20) || nt == 1) {
         rows(0, d);
         return;

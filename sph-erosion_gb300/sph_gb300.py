@@ -83,7 +83,8 @@ class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("wall_s", C.c_double), ("particle_steps", C.c_double),
                 ("throughput", C.c_double), ("p50_s", C.c_double), ("p99_s", C.c_double), ("max_s", C.c_double),
                 ("peak_bytes", C.c_int64), ("peak_active", C.c_int32), ("chunks", C.c_int32),
-                ("peak_particles", C.c_int64)]
+                ("peak_particles", C.c_int64), ("admit_s", C.c_double), ("prepare_s", C.c_double),
+                ("gpu_wait_s", C.c_double), ("retire_s", C.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
