@@ -206,8 +206,12 @@ def run_ours(args, spec, config):
     # variant from this state (each trial restarts from a snapshot; the
     # state is restored after)
     spin = spinup_steps(args)
-    if spin:
+    if args.load_state:
+        sc.load(args.load_state)  # a spun-up state saved by --save-state
+    elif spin:
         sysm.step(spin)
+    if args.save_state:
+        sc.save(args.save_state)
     for _ in range(args.warmup):
         sysm.step(1)
     sysm.sync()
@@ -302,9 +306,10 @@ def run_ours(args, spec, config):
 C_PARAMS_BYTES = 248 + 4
 
 # DRAM bytes (read + write) of one k_force launch, from an ncu capture of the
-# same workload with kernel variant 88 and cell_mult 0.5 (the neighbour lists
-# the force pass reads are most of it).  Reported only for that configuration.
-NCU_FORCE_TRAFFIC = {("plain_1m", 88, 0.5): 210.7e6}
+# same workload at the same point of the run (mid-run) with kernel variant 88
+# and cell_mult 0.5 (the neighbour lists the force pass reads are most of
+# it).  Reported only for that configuration.
+NCU_FORCE_TRAFFIC = {("plain_1m", 88, 0.5): 404.4e6}
 
 
 def _init_ranks():
@@ -463,6 +468,9 @@ def main():
     ap.add_argument("--spinup", type=int, default=None,
                     help="untimed steps before the warm-up (default: to mid-run; plain_1m 1000 of its 2000 steps, "
                          "skew 2000, batched 500, plain_small 500)")
+    ap.add_argument("--save-state", default=None, help="plain workloads: checkpoint the scene after the spin-up")
+    ap.add_argument("--load-state", default=None,
+                    help="plain workloads: start from a checkpoint instead of the spin-up (short profiler runs)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="warm-up and timed steps only (for profiler captures); prints nothing")
     args = ap.parse_args()
