@@ -283,6 +283,7 @@ def run_ours(args, spec, config):
                      "frac": achieved / hbm, "traffic": NCU_FORCE_TRAFFIC.get((config["workload"], variant, cm)),
                      "peak_kind": kind,
                      "step_bytes_frac": step_bytes / (step_ms * 1e-3) / 1e9 / hbm},
+        "issue_roofline": issue_roofline(config["workload"], variant, cm, force_ms, clk.summary()),
         "cpu_baseline": {"value": cpu_v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{m} of {n} particles x 3 all-pairs passes + integration per step"},
         "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": int(C_PARAMS_BYTES),
@@ -310,6 +311,28 @@ C_PARAMS_BYTES = 248 + 4
 # and cell_mult 0.5 (the neighbour lists the force pass reads are most of
 # it).  Reported only for that configuration.
 NCU_FORCE_TRAFFIC = {("plain_1m", 88, 0.5): 404.4e6}
+# Warp instructions of one k_force launch (smsp__inst_executed.sum) from the
+# same capture: with the live kernel time they place the kernel against the
+# instruction-issue roofline (4 warp instructions per cycle per SM).
+NCU_FORCE_WARP_INST = {("plain_1m", 88, 0.5): 397.26e6}
+
+
+def issue_roofline(workload, variant, cm, force_ms, clocks):
+    """The force kernel against the instruction-issue peak: warp
+    instructions per launch (ncu, same configuration and point of the run)
+    over the live CUDA-event time, against 4 per cycle per SM at the
+    sampled SM clock."""
+    inst = NCU_FORCE_WARP_INST.get((workload, variant, cm))
+    if inst is None or not force_ms:
+        return None
+    import torch
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    peak = 4.0 * sms * mhz * 1e6
+    achieved = inst / (force_ms * 1e-3)
+    return {"kernel": "k_force", "achieved": achieved, "peak": peak, "unit": "warp-instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_launch": inst, "source": "ncu smsp__inst_executed.sum"}
 
 
 def _init_ranks():
