@@ -145,6 +145,10 @@ SPH_API int sph_system_time_steps(sph_system* s, int nsteps, float* ms);
 SPH_API int sph_system_profile_stages(sph_system* s, int nsteps, float* ms);
 /* Bytes of device memory the system holds. */
 SPH_API int sph_system_memory(sph_system* s, int64_t* bytes);
+/* With no live scene, return the arenas' memory and go back to the initial
+ * capacities (arenas otherwise only grow); *trimmed = 0 when a scene is live.
+ * No counterpart in the reference. */
+SPH_API int sph_system_trim(sph_system* s, int* trimmed);
 
 /* Autotuner (no counterpart in the reference).  Times `steps` steps of the
  * system's current scenes under each candidate of particles per work tile

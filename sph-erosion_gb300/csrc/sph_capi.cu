@@ -162,6 +162,13 @@ int sph_system_memory(sph_system* s, int64_t* bytes) {
     });
 }
 
+int sph_system_trim(sph_system* s, int* trimmed) {
+    return guard([&] {
+        const bool t = sys(s).trim();
+        if (trimmed) *trimmed = t ? 1 : 0;
+    });
+}
+
 int sph_scene_create(sph_system* s, const sph_params* p, int capacity, int terrain_w, int terrain_d, int* scene) {
     return guard([&] {
         need(p, "params");

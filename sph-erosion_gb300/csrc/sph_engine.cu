@@ -194,11 +194,49 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
     diag_part_.resize((int64_t)kDiagBlocks * kDiagDoubles, false, st_);
     diag_i_.resize(2, false, st_);
     diag_nan_.resize(1, false, st_);
+    initial_arenas();
+}
+
+// Arena sizes of a fresh system (config capacities).
+void System::initial_arenas() {
     grow_particles(std::max<int64_t>(round_up(std::max<int64_t>(cfg_.particle_capacity, 1), kPAlign), kPAlign));
     grow_keys(std::max<int64_t>(round_up(std::max<int64_t>(cfg_.key_capacity, 1), kChunk), kChunk));
     grow_chunks(1024);
     grow_tables(4096);
     grow_terrain(std::max<int64_t>(round_up(std::max<int64_t>(cfg_.terrain_capacity, 1), kTAlign), kTAlign));
+}
+
+// With no live scene, return all arena memory and start again from the
+// initial sizes: arenas only grow, so after a peak of resident scenes their
+// free space would otherwise stay charged to the budget.
+bool System::trim() {
+    for (const Scene& sc : scenes_)
+        if (sc.live) return false;
+    SPH_CK(cudaStreamSynchronize(st_));
+    SPH_CK(cudaStreamSynchronize(cst_));
+    drop_graph();
+    DevBuf<float4>* f4[] = {&pos_, &vel_, &spos_, &svel_, &dyn_, &fdat_};
+    for (auto* b : f4) b->release();
+    DevBuf<uint32_t>* u4[] = {&key_, &slot_, &perm_, &nlist_, &counts_, &offsets_, &chunk_, &tab_};
+    for (auto* b : u4) b->release();
+    nbid_.release();
+    snbid_.release();
+    ncnt_.release();
+    rec_.release();
+    tbase_.release();
+    theight_.release();
+    tdelta_.release();
+    stage_.release();
+    scratch_i_.release();
+    for (auto& b : astage_) b.release();
+    pa_.reset(0);
+    ka_.reset(0);
+    ca_.reset(0);
+    ta_.reset(0);
+    tba_.reset(0);
+    initial_arenas();
+    work_dirty_ = true;
+    return true;
 }
 
 System::~System() {
@@ -510,16 +548,29 @@ int System::create_scene(const sph_params& p, int capacity, int tw, int td) {
     sc.p_cap = (int)round_up(std::max(capacity, 1), kPAlign);
     sc.tw = tw;
     sc.td = td;
-    check_budget(scene_bytes(sc.p_cap, tw, td, p));
+    // Arena growth is charged against the budget where it happens
+    // (ensure_arena); here only a scene that could never fit is refused.
+    if (cfg_.hbm_budget > 0 && scene_bytes(sc.p_cap, tw, td, p) > cfg_.hbm_budget)
+        throw Error(SPH_ERR_CAPACITY, "scene larger than the HBM budget");
     ensure_arena(pa_, sc.p_cap, 0);
     ensure_arena(ka_, sc.k_cap, 1);
     ensure_arena(ca_, sc.nchunks, 2);
     ensure_arena(tba_, sc.tab_len, 3);
     const int64_t tlen = tw > 0 ? round_up((int64_t)tw * td, kTAlign) : 0;
     if (tlen) ensure_arena(ta_, tlen, 4);
-    if (!pa_.alloc(sc.p_cap, &sc.p_off) || !ka_.alloc(sc.k_cap, &sc.k_off) || !ca_.alloc(sc.nchunks, &sc.c_off) ||
-        !tba_.alloc(sc.tab_len, &sc.tab_off) || (tlen && !ta_.alloc(tlen, &sc.t_off)))
-        throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+    {
+        // all ranges or none
+        bool okp = pa_.alloc(sc.p_cap, &sc.p_off), okk = okp && ka_.alloc(sc.k_cap, &sc.k_off);
+        bool okc = okk && ca_.alloc(sc.nchunks, &sc.c_off), okt = okc && tba_.alloc(sc.tab_len, &sc.tab_off);
+        bool oka = okt && (!tlen || ta_.alloc(tlen, &sc.t_off));
+        if (!oka) {
+            if (okt) tba_.release(sc.tab_off, sc.tab_len);
+            if (okc) ca_.release(sc.c_off, sc.nchunks);
+            if (okk) ka_.release(sc.k_off, sc.k_cap);
+            if (okp) pa_.release(sc.p_off, sc.p_cap);
+            throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+        }
+    }
     if (p.flags & SPH_FLAG_RECORD && rec_.n == 0) {
         rec_.resize(pos_.n * kRecFloats, false, st_);
         drop_graph();
@@ -571,16 +622,44 @@ void System::set_params(int id, const sph_params& p) {
         ka_.release(sc.k_off, sc.k_cap);
         ca_.release(sc.c_off, sc.nchunks);
         tba_.release(sc.tab_off, sc.tab_len);
-        ensure_arena(ka_, ng.k_cap, 1);
-        ensure_arena(ca_, ng.nchunks, 2);
-        ensure_arena(tba_, ng.tab_len, 3);
-        if (!ka_.alloc(ng.k_cap, &ng.k_off) || !ca_.alloc(ng.nchunks, &ng.c_off) || !tba_.alloc(ng.tab_len, &ng.tab_off))
-            throw Error(SPH_ERR_NOMEM, "arena allocation failed");
-        SPH_CK(cudaMemsetAsync(counts_.p + ng.k_off, 0, (size_t)ng.k_cap * 4, st_));
-        SPH_CK(cudaMemsetAsync(chunk_.p + ng.c_off, 0, (size_t)ng.nchunks * 4, st_));
+        // key ranges hold no state between steps (counts start from zero), so
+        // a refused resize re-acquires ranges for the old grid, wherever
+        // they land, and the scene keeps its old parameters
+        auto place = [&](Scene& g) {
+            ensure_arena(ka_, g.k_cap, 1);
+            ensure_arena(ca_, g.nchunks, 2);
+            ensure_arena(tba_, g.tab_len, 3);
+            int64_t ko, co, to;
+            if (!ka_.alloc(g.k_cap, &ko)) throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+            if (!ca_.alloc(g.nchunks, &co)) {
+                ka_.release(ko, g.k_cap);
+                throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+            }
+            if (!tba_.alloc(g.tab_len, &to)) {
+                ka_.release(ko, g.k_cap);
+                ca_.release(co, g.nchunks);
+                throw Error(SPH_ERR_NOMEM, "arena allocation failed");
+            }
+            g.k_off = ko;
+            g.c_off = co;
+            g.tab_off = to;
+            std::vector<uint32_t> tab(g.tab_len);
+            for (int y = 0; y < g.ny; ++y) tab[y] = yz_interleave(y, 0, g.by, g.bz);
+            for (int z = 0; z < g.nz; ++z) tab[g.ny + z] = yz_interleave(0, z, g.by, g.bz);
+            SPH_CK(cudaMemcpyAsync(tab_.p + g.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
+            SPH_CK(cudaMemsetAsync(counts_.p + g.k_off, 0, (size_t)g.k_cap * 4, st_));
+            SPH_CK(cudaMemsetAsync(chunk_.p + g.c_off, 0, (size_t)g.nchunks * 4, st_));
+        };
         work_dirty_ = true;
-    }
-    if (ng.nx != sc.nx || ng.ny != sc.ny || ng.nz != sc.nz || ng.tab_off != sc.tab_off) {
+        try {
+            place(ng);
+        } catch (...) {
+            place(sc);  // the space just released fits the old grid
+            upload_scene(id);
+            SPH_CK(cudaStreamSynchronize(st_));
+            throw;
+        }
+    } else if (ng.nx != sc.nx || ng.ny != sc.ny || ng.nz != sc.nz) {
         std::vector<uint32_t> tab(ng.tab_len);
         for (int y = 0; y < ng.ny; ++y) tab[y] = yz_interleave(y, 0, ng.by, ng.bz);
         for (int z = 0; z < ng.nz; ++z) tab[ng.ny + z] = yz_interleave(0, z, ng.by, ng.bz);

@@ -110,6 +110,7 @@ class System {
 
     void step(int nsteps);
     void sync();
+    bool trim();  // with no live scene: back to the initial arena sizes
     void autotune(int steps, sph_tune_result* out);
     float time_steps(int nsteps);
     void profile_stages(int nsteps, float* ms);
@@ -139,6 +140,7 @@ class System {
     void grow_chunks(int64_t cap);
     void rebuild_work();
     void ensure_nlist();
+    void initial_arenas();
     DevArrays arrays() const;
     LaunchShape shape() const;
     void enqueue_step(const DevArrays& a, const LaunchShape& s, cudaEvent_t* ev);

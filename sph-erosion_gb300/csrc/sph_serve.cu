@@ -174,6 +174,7 @@ class Server {
     void admit() {
         Range rg("sph/serve_admit");
         const double t = now();
+        bool trimmed = false;
         while (!queue_.empty() && queue_.front().arrival <= t) {
             Pending& q = queue_.front();
             const int64_t need = request_bytes(q.req);
@@ -188,8 +189,12 @@ class Server {
                 id = create_prepared(sys_, *q.prep);
             } catch (const Error& e) {
                 if (e.code == SPH_ERR_CAPACITY || e.code == SPH_ERR_NOMEM) {
-                    if (active_.empty()) throw;
-                    break;  // wait for retirements to free arena space
+                    if (!active_.empty()) break;  // wait for retirements to free arena space
+                    if (!trimmed && sys_.trim()) {  // nothing resident: shrink the arenas, retry once
+                        trimmed = true;
+                        continue;
+                    }
+                    throw;
                 }
                 throw;
             }

@@ -157,6 +157,7 @@ SIGNATURES = {
     "sph_scene_get_particles_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p]),
     "sph_host_alloc": (C.c_int, [C.c_int64, C.POINTER(C.c_void_p)]),
+    "sph_system_trim": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "sph_host_free": (C.c_int, [C.c_void_p]),
     "sph_grid_collision_u8": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -375,6 +376,13 @@ class System:
         r = TuneResult()
         _ck(lib().sph_system_autotune(self.h, int(steps), C.byref(r)))
         return r.as_dict()
+
+    def trim(self) -> bool:
+        """With no live scene, release the arenas' memory (back to the
+        initial capacities); False when a scene is live."""
+        t = C.c_int()
+        _ck(lib().sph_system_trim(self.h, C.byref(t)))
+        return bool(t.value)
 
     def memory(self) -> int:
         b = C.c_int64()

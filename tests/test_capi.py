@@ -72,3 +72,43 @@ def test_errors_are_status_codes(built_lib):
     assert L.sph_system_step(None, 1) == -1
     assert b"null" in L.sph_last_error()
     assert L.sph_scene_create(None, None, 0, 0, 0, None) == -1
+
+
+FRAME_LOOP_C = r"""
+#include <stddef.h>
+#include "sph_erosion.h"
+static void draw_instances(const float* p, int n) { (void)p; (void)n; }
+int frame_loop(int running) {
+    sph_system_config cfg; sph_system_config_default(&cfg);
+    sph_system* sys; if (sph_system_create(&cfg, &sys) != SPH_OK) return 1;
+    sph_params prm; sph_params_default(&prm);
+    prm.dt = 0.01f;
+    int sc; sph_scene_create(sys, &prm, 1000, 0, 0, &sc);
+    float origin[3] = {0, 0, 0}; int added;
+    sph_scene_add_lattice(sys, sc, 1000, origin, &added);
+    float* pos[2];
+    sph_host_alloc((int64_t)added * 12, (void**)&pos[0]);
+    sph_host_alloc((int64_t)added * 12, (void**)&pos[1]);
+    for (int frame = 0; frame < running; ++frame) {
+        sph_scene_set_params(sys, sc, &prm);
+        sph_system_step(sys, 1);
+        sph_scene_get_particles_async(sys, sc, pos[frame & 1], NULL, NULL, NULL);
+        sph_system_sync(sys);
+        draw_instances(pos[frame & 1], added);
+    }
+    sph_host_free(pos[0]); sph_host_free(pos[1]);
+    return sph_system_destroy(sys);
+}
+int main(void) { return 0; }  /* linked, not run: frame_loop needs a GPU */
+"""
+
+
+def test_frame_loop_example_compiles_as_c_and_links(built_lib, tmp_path):
+    """The per-frame loop shown for front ends compiles as C99 against the
+    header and links against the library."""
+    src = tmp_path / "loop.c"
+    src.write_text(FRAME_LOOP_C)
+    exe = tmp_path / "loop"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", f"-I{ROOT}/include", str(src), "-o", str(exe),
+                        f"-L{PKG}", "-lsph_gb300", f"-Wl,-rpath,{PKG}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

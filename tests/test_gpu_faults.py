@@ -51,3 +51,49 @@ def test_budget_too_small_refuses_scene():
         sc = sysm.scene_from_request(W.base_params(), dict(seed=3, particles=2000, terrain_side=64, steps=0))
         sysm.step(2)
         assert sc.diag()["total_units"] == 0
+
+
+def test_refused_grid_resize_keeps_the_scene_running():
+    """A parameter change whose finer grid does not fit the budget is refused
+    and the scene continues with its old parameters, bit for bit."""
+    req = dict(seed=11, particles=2000, terrain_side=64, steps=0)
+    with S.System() as probe:
+        sc = probe.scene_from_request(W.base_params(), req)
+        need = probe.memory()
+        probe.step(5)
+        want = sc.get_particles()["pos"]
+    with S.System(hbm_budget=need + (512 << 10)) as sysm:
+        sc = sysm.scene_from_request(W.base_params(), req)
+        p = sc.params()
+        old = p.cell_mult
+        p.cell_mult = 0.25
+        with pytest.raises(S.SphError) as e:
+            sc.set_params(p)
+        assert e.value.code == -4
+        assert sc.params().cell_mult == old
+        sysm.step(5)
+        assert np.array_equal(sc.get_particles()["pos"], want)
+
+
+def test_trim_returns_arena_memory_when_idle():
+    """Arenas only grow; with no live scene, trim returns their memory, so a
+    request with a different size mix fits a budget again."""
+    big_terrain = dict(seed=5, particles=4096, terrain_side=1024, steps=0)
+    many_particles = dict(seed=6, particles=120000, terrain_side=64, steps=0)
+    with S.System() as probe:
+        probe.scene_from_request(W.base_params(), many_particles)
+        need_b = probe.memory()
+    with S.System() as probe:
+        probe.scene_from_request(W.base_params(), big_terrain)
+        need_a = probe.memory()
+    budget = max(need_a, need_b) + (1 << 20)
+    with S.System(hbm_budget=budget) as sysm:
+        a = sysm.scene_from_request(W.base_params(), big_terrain)
+        assert not sysm.trim()  # a scene is live
+        a.destroy()
+        with pytest.raises(S.SphError):
+            sysm.scene_from_request(W.base_params(), many_particles)
+        assert sysm.trim()
+        b = sysm.scene_from_request(W.base_params(), many_particles)
+        sysm.step(2)
+        assert b.diag()["total_units"] == 0
