@@ -438,7 +438,8 @@ def run_serving(args, config):
     full = W.serving_trace(args.requests, rate=args.rate)
     trace = shard.shard_requests(full, ws, rank)
     with Clocks() as clk, S.Server(W.base_params(args.cell_mult), tile=args.tile, chunk_steps=16,
-                                    hbm_budget=120 << 30, device=local) as srv:
+                                    hbm_budget=120 << 30, device=local, policy=1 if args.policy == "work" else 0,
+                                    max_active_particles=args.max_active) as srv:
         res, st = srv.run_trace(trace)
     lat = [r.done_s - r.arrival_s for r in res]
     bad = sum(1 for r in res if r.total_units != 0 or r.nan_particles != 0)
@@ -459,7 +460,8 @@ def run_serving(args, config):
             "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Poisson request trace)",
             "config": dict(config, workload="serving", requests=len(full), rate_per_s=args.rate,
-                           hbm_budget_gb=120, parallelism=f"requests sharded over {ws} rank(s)"),
+                           hbm_budget_gb=120, parallelism=f"requests sharded over {ws} rank(s)",
+                           policy=args.policy, max_active_particles=args.max_active),
             "p50_latency_s": pct(0.50), "p99_latency_s": pct(0.99), "max_latency_s": float(lat[-1]),
             "wall_s": wall, "peak_active": max(q["peak"] for q in parts),
             "peak_particles": max(q["peak_p"] for q in parts), "peak_bytes": max(q["peak_b"] for q in parts),
@@ -487,6 +489,10 @@ def main():
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="serving: requests in the trace")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
+    ap.add_argument("--policy", default="work", choices=["arrival", "work"],
+                    help="serving: admission order among arrived requests (least work first by default)")
+    ap.add_argument("--max-active", type=int, default=40_000_000,
+                    help="serving: cap on resident particles (0 = none; the budget alone)")
     ap.add_argument("--particles", type=int, default=8388608, help="skew: particles (the box floor scales with them)")
     ap.add_argument("--spinup", type=int, default=None,
                     help="untimed steps before the warm-up (default: to mid-run; plain_1m 1000 of its 2000 steps, "

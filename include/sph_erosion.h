@@ -313,6 +313,8 @@ typedef struct sph_server_config {
     int64_t max_active_particles; /* admission cap on resident particles (0 = none) */
     int max_scenes;               /* 0 = 4096 */
     sph_params base;              /* physical constants of every scene */
+    int policy;                   /* admission order among arrived requests: 0 = arrival,
+                                     1 = least work (particles x steps) first */
 } sph_server_config;
 
 typedef struct sph_result {

@@ -29,16 +29,6 @@ int bits_for(int n) {
     return b;
 }
 
-uint32_t yz_interleave(int cy, int cz, int by, int bz) {
-    uint32_t m = 0;
-    int o = 0;
-    const int top = std::max(by, bz);
-    for (int b = 0; b < top; ++b) {
-        if (b < by) m |= (uint32_t)((cy >> b) & 1) << o++;
-        if (b < bz) m |= (uint32_t)((cz >> b) & 1) << o++;
-    }
-    return m;
-}
 
 inline float bits_to_float(int v) {
     float f;
@@ -52,6 +42,19 @@ inline int float_to_bits(float f) {
 }
 
 }  // namespace
+
+// (y, z) Morton interleave of the row index: bit b of y, then bit b of z,
+// while each coordinate still has bits.
+uint32_t yz_interleave(int cy, int cz, int by, int bz) {
+    uint32_t m = 0;
+    int o = 0;
+    const int top = std::max(by, bz);
+    for (int b = 0; b < top; ++b) {
+        if (b < by) m |= (uint32_t)((cy >> b) & 1) << o++;
+        if (b < bz) m |= (uint32_t)((cz >> b) & 1) << o++;
+    }
+    return m;
+}
 
 // Largest float s with sqrtf(s) <= h.  sqrtf is correctly rounded and
 // monotonic, so for every float s >= 0: sqrtf(s) <= h  <=>  s <= smax.  The
@@ -284,13 +287,14 @@ int64_t System::memory_bytes() const {
 }
 
 // Bytes one scene of n particles and a tw x td terrain needs in the arenas.
-int64_t System::scene_bytes(int n, int tw, int td, const sph_params& p) const {
+int64_t System::scene_bytes(int n, int tw, int td, const sph_params& p, bool lists) const {
     Scene tmp;
     tmp.prm = p;
     const_cast<System*>(this)->geometry(tmp);
     const int64_t pcap = round_up(std::max(n, 1), kPAlign);
     int64_t per_p = 5 * 16 + 3 * 4 + 2 * 4 + ((p.flags & SPH_FLAG_RECORD) ? kRecFloats * 4 : 0);
-    if (cfg_.variant & 8) per_p += (int64_t)kNbCap * 4 + 4 + ((cfg_.variant & 128) ? 32 : 0);  // neighbour lists
+    if (lists && (cfg_.variant & 8))  // neighbour lists: optional, dropped when the budget has no room
+        per_p += (int64_t)kNbCap * 4 + 4 + ((cfg_.variant & 128) ? 32 : 0);
     return pcap * per_p + (int64_t)tmp.k_cap * 8 + (int64_t)tmp.nchunks * 4 + tmp.tab_len * 4 +
            round_up((int64_t)tw * td, kTAlign) * 16 + (int64_t)(pcap / cfg_.tile + tmp.nchunks) * 8;
 }
@@ -550,7 +554,7 @@ int System::create_scene(const sph_params& p, int capacity, int tw, int td) {
     sc.td = td;
     // Arena growth is charged against the budget where it happens
     // (ensure_arena); here only a scene that could never fit is refused.
-    if (cfg_.hbm_budget > 0 && scene_bytes(sc.p_cap, tw, td, p) > cfg_.hbm_budget)
+    if (cfg_.hbm_budget > 0 && scene_bytes(sc.p_cap, tw, td, p, false) > cfg_.hbm_budget)
         throw Error(SPH_ERR_CAPACITY, "scene larger than the HBM budget");
     ensure_arena(pa_, sc.p_cap, 0);
     ensure_arena(ka_, sc.k_cap, 1);

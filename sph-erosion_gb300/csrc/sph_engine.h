@@ -117,7 +117,8 @@ class System {
     int64_t memory_bytes() const;
     int num_scenes() const { return (int)scenes_.size(); }
     bool scene_live(int id) const { return id >= 0 && id < (int)scenes_.size() && scenes_[id].live; }
-    int64_t scene_bytes(int n, int tw, int td, const sph_params& p) const;
+    // Arena bytes of a scene; `lists`: with the optional neighbour lists.
+    int64_t scene_bytes(int n, int tw, int td, const sph_params& p, bool lists = true) const;
     cudaStream_t stream() const { return st_; }
     unsigned read_status();
     void check_status();
@@ -208,6 +209,8 @@ void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, floa
 
 // Sets the calling thread's sph_last_error() message (sph_capi.cu).
 void set_last_error(const std::string& msg);
+// Interleave-table entry of a grid row: the (y, z) Morton index.
+uint32_t yz_interleave(int cy, int cz, int by, int bz);
 
 // Terrain meshes (sph_mesh.cu).
 void mesh_u8(const unsigned char* map_host, int dimx, int dimy, int dimz, float* verts, unsigned* idx,

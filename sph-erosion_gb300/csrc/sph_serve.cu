@@ -11,6 +11,7 @@
 #include <chrono>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <string>
 #include <thread>
@@ -81,6 +82,7 @@ class Server {
         if (cfg_.chunk_steps <= 0) cfg_.chunk_steps = 16;
         if (cfg_.hbm_budget <= 0) cfg_.hbm_budget = (int64_t)120 << 30;
         if (cfg_.cell_mult <= 0.0f) cfg_.cell_mult = 0.5f;
+        if (cfg_.policy != 0 && cfg_.policy != 1) throw Error(SPH_ERR_INVALID, "policy must be 0 (arrival) or 1 (work)");
         cfg_.base.cell_mult = cfg_.cell_mult;
     }
 
@@ -120,11 +122,11 @@ class Server {
             retire();
             lap(&stats_.retire_s);
         }
-        return (int)(queue_.size() + active_.size());
+        return (int)(queue_.size() + ready_.size() + active_.size());
     }
 
     bool idle_until_arrival(double* next) const {
-        if (!active_.empty() || queue_.empty()) return false;
+        if (!active_.empty() || !ready_.empty() || queue_.empty()) return false;
         *next = queue_.front().arrival;
         return true;
     }
@@ -175,8 +177,10 @@ class Server {
         Range rg("sph/serve_admit");
         const double t = now();
         bool trimmed = false;
-        while (!queue_.empty() && queue_.front().arrival <= t) {
-            Pending& q = queue_.front();
+        collect_arrivals(t);
+        while (!ready_.empty()) {
+            const auto it = ready_.begin();
+            Pending& q = it->second;
             const int64_t need = request_bytes(q.req);
             if (need > cfg_.hbm_budget) throw Error(SPH_ERR_CAPACITY, "a request exceeds the whole HBM budget");
             if (reserved_ + need > cfg_.hbm_budget) break;
@@ -203,11 +207,24 @@ class Server {
             active_.push_back(Active{Pending{q.ticket, q.req, q.arrival, nullptr, 0}, id, now(), need});
             reserved_ += need;
             resident_particles_ += q.req.particles;
-            queue_.pop_front();
+            const bool retire_next = q.req.steps == 0;
+            ready_.erase(it);
             stats_.peak_active = std::max<int32_t>(stats_.peak_active, (int32_t)active_.size());
             stats_.peak_particles = std::max<int64_t>(stats_.peak_particles, resident_particles_);
             stats_.peak_bytes = std::max<int64_t>(stats_.peak_bytes, sys_.memory_bytes());
-            if (q.req.steps == 0) break;  // retire it on the next round
+            if (retire_next) break;  // retire it on the next round
+        }
+    }
+
+    // Move the requests that have arrived by time t into the ready set,
+    // ordered by arrival (policy 0) or by work, particles x steps (policy 1).
+    void collect_arrivals(double t) {
+        while (!queue_.empty() && queue_.front().arrival <= t) {
+            Pending& q = queue_.front();
+            const double key = cfg_.policy == 1 ? (double)q.req.particles * (double)std::max(q.req.steps, 1)
+                                                : q.arrival;
+            ready_.emplace(key, std::move(q));
+            queue_.pop_front();
         }
     }
 
@@ -221,12 +238,13 @@ class Server {
     static constexpr int kPrepareAhead = 256;
     static constexpr int64_t kPrepareBytes = (int64_t)1 << 30;
     void prepare_ahead() {
-        const double t = now();
+        collect_arrivals(now());
         std::vector<Pending*> todo;
         int64_t bytes = prepared_bytes_;
         int held = 0;
-        for (Pending& q : queue_) {
-            if (q.arrival > t || held >= kPrepareAhead || bytes >= kPrepareBytes) break;
+        for (auto& kv : ready_) {
+            Pending& q = kv.second;
+            if (held >= kPrepareAhead || bytes >= kPrepareBytes) break;
             ++held;
             if (q.prep) continue;
             todo.push_back(&q);
@@ -301,7 +319,8 @@ class Server {
     sph_server_config cfg_;
     System sys_;
     Clock::time_point t0_;
-    std::deque<Pending> queue_;
+    std::deque<Pending> queue_;                // not yet arrived, by arrival time
+    std::multimap<double, Pending> ready_;     // arrived, in admission order
     std::vector<Active> active_;
     std::vector<sph_result> done_;
     int64_t next_ticket_ = 1;

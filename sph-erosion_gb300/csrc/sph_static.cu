@@ -140,22 +140,8 @@ extern "C" SPH_API int sph_density_static(const sph_params* p, int n, const floa
         for (int t = 0; t * kStaticTile < n; ++t) pt.push_back({0, t * kStaticTile});
         for (int c = 0; c < sc.nchunks; ++c) ct.push_back({0, c});
         std::vector<uint32_t> tab(sc.tab_len);
-        for (int y = 0; y < sc.ny; ++y) {
-            uint32_t m = 0;
-            for (int b = 0, o = 0; b < std::max(sc.by, sc.bz); ++b) {
-                if (b < sc.by) m |= (uint32_t)((y >> b) & 1) << o;
-                o += (b < sc.by) + (b < sc.bz);
-            }
-            tab[y] = m;
-        }
-        for (int z = 0; z < sc.nz; ++z) {
-            uint32_t m = 0;
-            for (int b = 0, o = 0; b < std::max(sc.by, sc.bz); ++b) {
-                if (b < sc.by) ++o;
-                if (b < sc.bz) m |= (uint32_t)((z >> b) & 1) << o++;
-            }
-            tab[sc.ny + z] = m;
-        }
+        for (int y = 0; y < sc.ny; ++y) tab[y] = yz_interleave(y, 0, sc.by, sc.bz);
+        for (int z = 0; z < sc.nz; ++z) tab[sc.ny + z] = yz_interleave(0, z, sc.by, sc.bz);
         const int steps = -1;
         const int nwork[4] = {(int)pt.size(), (int)ct.size(), 0, 0};
         check_cuda(cudaMemcpyAsync(base + kOffScene, &sc.dev, sizeof(SceneDev), cudaMemcpyHostToDevice, st), "copy");

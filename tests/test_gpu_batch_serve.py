@@ -164,3 +164,21 @@ def test_async_readback_matches_sync():
         for b in bufs:
             ref.step(3)
             assert np.array_equal(b, rs.get_positions())
+
+
+def test_server_least_work_first_policy():
+    """Policy 1 admits the arrived request with the least work (particles x
+    steps) first: with room for one request at a time, all arriving at once,
+    they complete in order of work, each with the same state as served in
+    arrival order."""
+    spec = [(20000, 64), (3000, 16), (8000, 32), (2500, 8)]
+    reqs = [dict(seed=300 + i, particles=p, terrain_side=64, steps=st, arrival_s=0.0) for i, (p, st) in enumerate(spec)]
+    hashes = {}
+    for policy in (1, 0):
+        with S.Server(W.base_params(), chunk_steps=8, policy=policy, max_active_particles=1) as srv:
+            res, _ = srv.run_trace(reqs)
+        hashes[policy] = [r.state_hash for r in res]
+        if policy == 1:
+            by_done = sorted(range(len(res)), key=lambda i: res[i].done_s)
+            assert by_done == sorted(range(len(spec)), key=lambda i: spec[i][0] * spec[i][1])
+    assert hashes[0] == hashes[1]
