@@ -97,3 +97,14 @@ def test_trim_returns_arena_memory_when_idle():
         b = sysm.scene_from_request(W.base_params(), many_particles)
         sysm.step(2)
         assert b.diag()["total_units"] == 0
+
+
+def test_grid_beyond_key_limit_is_refused():
+    """A box whose uniform grid would need more than 2^30 cell keys is
+    refused with an error code; a coarser cell size makes it fit."""
+    with S.System() as sysm:
+        with pytest.raises(S.SphError) as e:
+            sysm.scene(S.default_params(**dict(W.PHYS, box_half=(60.0, 60.0, 60.0))))
+        assert e.value.code == -4
+        sc = sysm.scene(S.default_params(**dict(W.PHYS, box_half=(10.0, 1.0, 10.0), cell_mult=1.0)))
+        assert sc.grid_dims()[3] <= (1 << 30) + 1
