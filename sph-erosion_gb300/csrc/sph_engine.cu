@@ -182,6 +182,9 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
         SPH_CK(cudaEventCreateWithFlags(&gathered_[k], cudaEventDisableTiming));
         SPH_CK(cudaEventCreateWithFlags(&copied_[k], cudaEventDisableTiming));
     }
+    SPH_CK(cudaMallocHost(&up_dev_, sizeof(SceneDev) * kUploadRing));
+    SPH_CK(cudaMallocHost(&up_steps_, sizeof(int) * kUploadRing));
+    for (auto& e : up_ev_) SPH_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     configure_kernels();
     SPH_CK(cudaGetLastError());
     pa_.reset(0);
@@ -252,6 +255,10 @@ System::~System() {
         if (copied_[k]) cudaEventDestroy(copied_[k]);
     }
     if (cst_) cudaStreamDestroy(cst_);
+    for (auto& e : up_ev_)
+        if (e) cudaEventDestroy(e);
+    if (up_dev_) cudaFreeHost(up_dev_);
+    if (up_steps_) cudaFreeHost(up_steps_);
     DevBuf<float4>* f4[] = {&pos_, &vel_, &spos_, &svel_, &dyn_};
     for (auto* b : f4) b->release();
     key_.release(); slot_.release(); perm_.release();
@@ -512,13 +519,20 @@ void System::fill_dev(Scene& sc) {
 }
 
 // Stream-ordered: kernels enqueued before see the old descriptor, later ones
-// the new.  The sources are pageable host memory, which the copy stages
-// before returning, so the host may change them right after.
+// the new.  The copy reads a pinned ring slot, so it does not make the host
+// wait for the stream (a copy from pageable memory may); a slot is rewritten
+// only after the copy that read it has run.
 void System::upload_scene(int id) {
     Scene& sc = scenes_[id];
     fill_dev(sc);
-    SPH_CK(cudaMemcpyAsync(dscenes_.p + id, &sc.dev, sizeof(SceneDev), cudaMemcpyHostToDevice, st_));
-    SPH_CK(cudaMemcpyAsync(steps_.p + id, &sc.steps, sizeof(int), cudaMemcpyHostToDevice, st_));
+    const int k = up_next_;
+    up_next_ = (up_next_ + 1) % kUploadRing;
+    SPH_CK(cudaEventSynchronize(up_ev_[k]));
+    up_dev_[k] = sc.dev;
+    up_steps_[k] = sc.steps;
+    SPH_CK(cudaMemcpyAsync(dscenes_.p + id, up_dev_ + k, sizeof(SceneDev), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemcpyAsync(steps_.p + id, up_steps_ + k, sizeof(int), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaEventRecord(up_ev_[k], st_));
 }
 
 static void validate(const sph_params& p) {

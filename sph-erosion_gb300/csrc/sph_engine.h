@@ -153,6 +153,14 @@ class System {
     void upload_terrain_height(Scene& sc);
 
     sph_system_config cfg_;
+    // scene-descriptor uploads from a ring of pinned slots (a slot is reused
+    // once the copy that read it has run), so set_params never waits for the
+    // stream
+    static constexpr int kUploadRing = 64;
+    SceneDev* up_dev_ = nullptr;  // pinned, kUploadRing entries
+    int* up_steps_ = nullptr;     // pinned, kUploadRing entries
+    cudaEvent_t up_ev_[kUploadRing] = {};
+    int up_next_ = 0;
     // asynchronous readback: gathers on st_ into one of two staging buffers,
     // device-to-host copies on cst_
     cudaStream_t cst_ = nullptr;
