@@ -304,6 +304,7 @@ def run_ours(args, spec, config):
         "gpu_launches": int(args.steps * (7 if t else 6)),
         "stages_ms": {name: float(v) for name, v in zip(S.STAGES, stages)},
         "clocks": clk.summary(),
+        "device_bytes": int(sysm.memory()),
         "mass_units_total": int(d["total_units"]),
         "diag_fp64": {"kinetic": d["kinetic"], "potential": d["potential"], "momentum": d["momentum"],
                       "nan_particles": d["nan_particles"]},
