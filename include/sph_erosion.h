@@ -97,6 +97,10 @@ typedef struct sph_diag {
     double unit_volume;      /* m^3 per unit */
     int32_t n;               /* particles */
     int32_t nan_particles;   /* particles with a non-finite position */
+    uint64_t state_hash;     /* fingerprint of the particle state: the sum (mod 2^64) over
+                                particles of a 64-bit mix (splitmix64 finaliser) of the id and
+                                the bits of position, velocity and sediment; equal states give
+                                equal fingerprints whatever their order in memory */
 } sph_diag;
 
 typedef struct sph_system_config {
@@ -215,6 +219,8 @@ SPH_API int sph_scene_get_particle(sph_system* s, int scene, int id, sph_particl
  * pos3 vel3 acc3 density pressure fpress3 fvisc3 fgrav3 fsurf3 normal3 pad. */
 SPH_API int sph_scene_get_records(sph_system* s, int scene, float* rec27, int* neighb_id);
 SPH_API int sph_scene_diag(sph_system* s, int scene, sph_diag* out);
+/* The same for k scenes in one launch (k <= max_scenes): out[i] for scenes[i]. */
+SPH_API int sph_scenes_diag(sph_system* s, int k, const int* scenes, sph_diag* out);
 
 /* ---- terrain (Grid heightfield, grid.h:43-116) ---------------------------- */
 /* LoadHeightfield generalised to any size and FP32 metres above the box floor
@@ -328,7 +334,7 @@ typedef struct sph_result {
     int32_t nan_particles;
     int32_t pad;
     double kinetic;
-    uint64_t state_hash;               /* FNV-1a of final positions, velocities, sediment in id order */
+    uint64_t state_hash;               /* sph_diag.state_hash of the final state */
 } sph_result;
 
 typedef struct sph_server_stats {

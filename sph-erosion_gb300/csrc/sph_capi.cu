@@ -287,6 +287,16 @@ int sph_scene_diag(sph_system* s, int scene, sph_diag* out) {
     });
 }
 
+int sph_scenes_diag(sph_system* s, int k, const int* scenes, sph_diag* out) {
+    return guard([&] {
+        if (k < 0) throw sph::Error(SPH_ERR_INVALID, "negative scene count");
+        if (k == 0) return;
+        need(scenes, "scenes");
+        need(out, "out");
+        sys(s).diag_many(scenes, k, out);
+    });
+}
+
 int sph_scene_set_terrain(sph_system* s, int scene, int w, int d, const float* heights) {
     return guard([&] { sys(s).set_terrain(scene, w, d, heights); });
 }

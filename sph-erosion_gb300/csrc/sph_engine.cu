@@ -198,7 +198,7 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
     slist_.resize(cfg_.max_scenes, false, st_);
     status_.resize(1, false, st_);
     diag_part_.resize((int64_t)kDiagBlocks * kDiagDoubles, false, st_);
-    diag_i_.resize(2, false, st_);
+    diag_i_.resize(3, false, st_);
     diag_nan_.resize(1, false, st_);
     initial_arenas();
 }
@@ -878,37 +878,52 @@ void System::get_records(int id, float* rec27, int* nbid, int32_t* sed) {
     }
 }
 
-void System::diag(int id, sph_diag* out) {
-    Scene& sc = scene(id);
+void System::diag(int id, sph_diag* out) { diag_many(&id, 1, out); }
+
+// FP64 diagnostics, mass units and state fingerprints of k scenes: one
+// launch, one set of copies, one wait.
+void System::diag_many(const int* ids, int k, sph_diag* out) {
+    if (k > cfg_.max_scenes) throw Error(SPH_ERR_INVALID, "more scenes than the system holds");
+    for (int q = 0; q < k; ++q) scene(ids[q]);
     if (work_dirty_) rebuild_work();
-    SPH_CK(cudaMemcpyAsync(slist_.p, &id, sizeof(int), cudaMemcpyHostToDevice, st_));
-    SPH_CK(cudaMemsetAsync(diag_i_.p, 0, 2 * sizeof(long long), st_));
-    SPH_CK(cudaMemsetAsync(diag_nan_.p, 0, sizeof(int), st_));
-    launch_diag(arrays(), 1, diag_part_.p, diag_i_.p, diag_nan_.p, st_);
+    if (diag_part_.n < (int64_t)k * kDiagBlocks * kDiagDoubles)
+        diag_part_.resize((int64_t)k * kDiagBlocks * kDiagDoubles, false, st_);
+    if (diag_i_.n < (int64_t)3 * k) diag_i_.resize((int64_t)3 * k, false, st_);
+    if (diag_nan_.n < k) diag_nan_.resize(k, false, st_);
+    SPH_CK(cudaMemcpyAsync(slist_.p, ids, (size_t)k * sizeof(int), cudaMemcpyHostToDevice, st_));
+    SPH_CK(cudaMemsetAsync(diag_i_.p, 0, (size_t)3 * k * sizeof(long long), st_));
+    SPH_CK(cudaMemsetAsync(diag_nan_.p, 0, (size_t)k * sizeof(int), st_));
+    launch_diag(arrays(), k, diag_part_.p, diag_i_.p, diag_nan_.p, st_);
     SPH_CK(cudaGetLastError());
-    std::vector<double> part((size_t)kDiagBlocks * kDiagDoubles);
-    long long is[2];
-    int nan = 0;
+    std::vector<double> part((size_t)k * kDiagBlocks * kDiagDoubles);
+    std::vector<long long> is((size_t)3 * k);
+    std::vector<int> nan(k);
     SPH_CK(cudaMemcpyAsync(part.data(), diag_part_.p, part.size() * 8, cudaMemcpyDeviceToHost, st_));
-    SPH_CK(cudaMemcpyAsync(is, diag_i_.p, sizeof is, cudaMemcpyDeviceToHost, st_));
-    SPH_CK(cudaMemcpyAsync(&nan, diag_nan_.p, sizeof nan, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(is.data(), diag_i_.p, is.size() * 8, cudaMemcpyDeviceToHost, st_));
+    SPH_CK(cudaMemcpyAsync(nan.data(), diag_nan_.p, nan.size() * 4, cudaMemcpyDeviceToHost, st_));
     SPH_CK(cudaStreamSynchronize(st_));
-    double acc[kDiagDoubles] = {0};
-    for (int b = 0; b < kDiagBlocks; ++b)
-        for (int c = 0; c < kDiagDoubles; ++c) acc[c] += part[(size_t)b * kDiagDoubles + c];
-    std::memset(out, 0, sizeof *out);
-    out->fluid_mass = (double)sc.n * (double)sc.prm.mass;
-    out->momentum[0] = acc[0];
-    out->momentum[1] = acc[1];
-    out->momentum[2] = acc[2];
-    out->kinetic = acc[3];
-    out->potential = acc[4];
-    out->sediment_units = is[0];
-    out->terrain_units = is[1];
-    out->total_units = is[0] + is[1];
-    out->unit_volume = ((double)sc.prm.mass / (double)sc.prm.rest_density) * std::ldexp(1.0, -30);
-    out->n = sc.n;
-    out->nan_particles = nan;
+    for (int q = 0; q < k; ++q) {
+        const Scene& sc = scene(ids[q]);
+        double acc[kDiagDoubles] = {0};
+        for (int b = 0; b < kDiagBlocks; ++b)
+            for (int c = 0; c < kDiagDoubles; ++c)
+                acc[c] += part[((size_t)q * kDiagBlocks + b) * kDiagDoubles + c];
+        sph_diag* o = out + q;
+        std::memset(o, 0, sizeof *o);
+        o->fluid_mass = (double)sc.n * (double)sc.prm.mass;
+        o->momentum[0] = acc[0];
+        o->momentum[1] = acc[1];
+        o->momentum[2] = acc[2];
+        o->kinetic = acc[3];
+        o->potential = acc[4];
+        o->sediment_units = is[3 * q];
+        o->terrain_units = is[3 * q + 1];
+        o->total_units = is[3 * q] + is[3 * q + 1];
+        o->unit_volume = ((double)sc.prm.mass / (double)sc.prm.rest_density) * std::ldexp(1.0, -30);
+        o->n = sc.n;
+        o->nan_particles = nan[q];
+        o->state_hash = (uint64_t)is[3 * q + 2];
+    }
 }
 
 void System::upload_terrain_height(Scene& sc) {

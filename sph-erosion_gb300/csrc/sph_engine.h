@@ -96,6 +96,7 @@ class System {
     void get_particles_async(int id, float* pos3, float* vel3, float* density, int32_t* sed);
     void get_records(int id, float* rec27, int* nbid, int32_t* sed);
     void diag(int id, sph_diag* out);
+    void diag_many(const int* ids, int k, sph_diag* out);
     void set_terrain(int id, int w, int d, const float* heights);
     void gen_terrain(int id, uint64_t seed, int octaves, float amp, float lac, float gain, int kind);
     void get_terrain(int id, float* heights, int64_t* delta);

@@ -974,9 +974,26 @@ __global__ void __launch_bounds__(kMaxTile) k_neighbour_counts(DevArrays a, int3
     }
 }
 
+// splitmix64's finaliser (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ unsigned long long pair64(float lo, float hi) {
+    return (unsigned long long)(uint32_t)__float_as_int(lo) |
+           ((unsigned long long)(uint32_t)__float_as_int(hi) << 32);
+}
+
 // FP64 diagnostics: kDiagBlocks blocks per listed scene write fixed-order
-// partial sums (so the result is reproducible); integer totals use int64
-// atomics, which are exact in any order.
+// partial sums of momentum and energies (so the result is reproducible);
+// integer totals use int64 atomics, which are exact in any order: sediment
+// and terrain units, non-finite positions and the state fingerprint (sum of
+// a mix of each particle's id and state bits, so any order of the particles
+// in memory gives the same value).  isums holds three values per listed
+// scene.
 __global__ void __launch_bounds__(256) k_diag(DevArrays a, double* partial, long long* isums, int* nan_count) {
     __shared__ double sh[kDiagDoubles][8];
     const int li = blockIdx.x / kDiagBlocks, b = blockIdx.x % kDiagBlocks;
@@ -984,11 +1001,18 @@ __global__ void __launch_bounds__(256) k_diag(DevArrays a, double* partial, long
     const SceneDev& S = a.scenes[sidx];
     double acc[kDiagDoubles] = {0, 0, 0, 0, 0, 0, 0, 0};
     long long sed = 0, ter = 0;
+    unsigned long long fp = 0;
     int nan = 0;
     const double m = (double)S.mass;
     for (int q = b * 256 + threadIdx.x; q < S.n; q += kDiagBlocks * 256) {
         const float4 x = a.pos[S.p_off + q];
         const float4 v = a.vel[S.p_off + q];
+        unsigned long long h = mix64(0x9e3779b97f4a7c15ULL * (unsigned long long)(uint32_t)(__float_as_int(x.w) + 1));
+        h = mix64(h ^ pair64(x.x, x.y));
+        h = mix64(h ^ pair64(x.z, v.x));
+        h = mix64(h ^ pair64(v.y, v.z));
+        h = mix64(h ^ (unsigned long long)(uint32_t)__float_as_int(v.w));
+        fp += h;
         const double vx = v.x, vy = v.y, vz = v.z;
         acc[0] += m * vx;
         acc[1] += m * vy;
@@ -1014,11 +1038,14 @@ __global__ void __launch_bounds__(256) k_diag(DevArrays a, double* partial, long
     for (int o = 16; o > 0; o >>= 1) {
         sed += __shfl_down_sync(kFull, sed, o);
         ter += __shfl_down_sync(kFull, ter, o);
+        fp += __shfl_down_sync(kFull, fp, o);
         nan += __shfl_down_sync(kFull, nan, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        if (sed) atomicAdd(reinterpret_cast<unsigned long long*>(isums + 2 * li), (unsigned long long)sed);
-        if (ter) atomicAdd(reinterpret_cast<unsigned long long*>(isums + 2 * li + 1), (unsigned long long)ter);
+        unsigned long long* u = reinterpret_cast<unsigned long long*>(isums + 3 * li);
+        if (sed) atomicAdd(u, (unsigned long long)sed);
+        if (ter) atomicAdd(u + 1, (unsigned long long)ter);
+        if (fp) atomicAdd(u + 2, fp);
         if (nan) atomicAdd(nan_count + li, nan);
     }
 }

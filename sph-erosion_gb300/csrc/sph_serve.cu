@@ -27,15 +27,6 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
-    const unsigned char* b = static_cast<const unsigned char*>(p);
-    for (size_t i = 0; i < n; ++i) {
-        h ^= b[i];
-        h *= 0x100000001B3ULL;
-    }
-    return h;
-}
-
 }  // namespace
 
 // Host-side inputs of a request's scene: parameters, particles, terrain.
@@ -273,45 +264,42 @@ class Server {
         }
     }
 
+    // Retire every finished scene: one diagnostic launch for all of them
+    // (mass units, FP64 energies and the state fingerprint), then free their
+    // ranges for the next admission.
     void retire() {
         Range rg("sph/serve_retire");
         const double t = now();
-        std::vector<Active> keep;
-        for (Active& a : active_) {
-            if (sys_.steps(a.scene) > 0) {
-                keep.push_back(a);
-                continue;
+        std::vector<Active> keep, fin;
+        for (Active& a : active_) (sys_.steps(a.scene) > 0 ? keep : fin).push_back(a);
+        if (!fin.empty()) {
+            std::vector<int> ids(fin.size());
+            for (size_t q = 0; q < fin.size(); ++q) ids[q] = fin[q].scene;
+            std::vector<sph_diag> d(fin.size());
+            sys_.diag_many(ids.data(), (int)ids.size(), d.data());
+            for (size_t q = 0; q < fin.size(); ++q) {
+                const Active& a = fin[q];
+                sph_result r;
+                std::memset(&r, 0, sizeof r);
+                r.ticket = a.p.ticket;
+                r.seed = a.p.req.seed;
+                r.particles = a.p.req.particles;
+                r.steps = a.p.req.steps;
+                r.arrival_s = a.p.arrival;
+                r.admit_s = a.admit;
+                r.done_s = t;
+                r.total_units = d[q].total_units;
+                r.sediment_units = d[q].sediment_units;
+                r.nan_particles = d[q].nan_particles;
+                r.kinetic = d[q].kinetic;
+                r.state_hash = d[q].state_hash;
+                sys_.destroy_scene(a.scene);
+                reserved_ -= a.bytes;
+                resident_particles_ -= a.p.req.particles;
+                done_.push_back(r);
+                stats_.completed += 1;
+                stats_.particle_steps += (double)a.p.req.particles * (double)a.p.req.steps;
             }
-            sph_result r;
-            std::memset(&r, 0, sizeof r);
-            r.ticket = a.p.ticket;
-            r.seed = a.p.req.seed;
-            r.particles = a.p.req.particles;
-            r.steps = a.p.req.steps;
-            r.arrival_s = a.p.arrival;
-            r.admit_s = a.admit;
-            r.done_s = t;
-            sph_diag d;
-            sys_.diag(a.scene, &d);
-            r.total_units = d.total_units;
-            r.sediment_units = d.sediment_units;
-            r.nan_particles = d.nan_particles;
-            r.kinetic = d.kinetic;
-            const int n = a.p.req.particles;
-            std::vector<float> pos((size_t)n * 3), vel((size_t)n * 3);
-            std::vector<int32_t> sed(n);
-            sys_.get_particles(a.scene, pos.data(), vel.data(), nullptr, sed.data());
-            uint64_t h = 0xCBF29CE484222325ULL;
-            h = fnv1a(h, pos.data(), pos.size() * 4);
-            h = fnv1a(h, vel.data(), vel.size() * 4);
-            h = fnv1a(h, sed.data(), sed.size() * 4);
-            r.state_hash = h;
-            sys_.destroy_scene(a.scene);
-            reserved_ -= a.bytes;
-            resident_particles_ -= a.p.req.particles;
-            done_.push_back(r);
-            stats_.completed += 1;
-            stats_.particle_steps += (double)a.p.req.particles * (double)a.p.req.steps;
         }
         active_.swap(keep);
     }

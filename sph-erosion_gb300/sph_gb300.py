@@ -50,13 +50,15 @@ class Diag(C.Structure):
         ("fluid_mass", C.c_double), ("momentum", C.c_double * 3), ("kinetic", C.c_double),
         ("potential", C.c_double), ("sediment_units", C.c_int64), ("terrain_units", C.c_int64),
         ("total_units", C.c_int64), ("unit_volume", C.c_double), ("n", C.c_int32), ("nan_particles", C.c_int32),
+        ("state_hash", C.c_uint64),
     ]
 
     def as_dict(self):
         return {"fluid_mass": self.fluid_mass, "momentum": tuple(self.momentum), "kinetic": self.kinetic,
                 "potential": self.potential, "sediment_units": self.sediment_units,
                 "terrain_units": self.terrain_units, "total_units": self.total_units,
-                "unit_volume": self.unit_volume, "n": self.n, "nan_particles": self.nan_particles}
+                "unit_volume": self.unit_volume, "n": self.n, "nan_particles": self.nan_particles,
+                "state_hash": self.state_hash}
 
 
 class SystemConfig(C.Structure):
@@ -138,6 +140,7 @@ SIGNATURES = {
     "sph_scene_get_particle": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(Particle)]),
     "sph_scene_get_records": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "sph_scene_diag": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Diag)]),
+    "sph_scenes_diag": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(Diag)]),
     "sph_scene_set_terrain": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "sph_scene_gen_terrain": (C.c_int, [C.c_void_p, C.c_int, C.c_uint64, C.c_int, C.c_float, C.c_float, C.c_float,
                                         C.c_int]),
@@ -384,6 +387,16 @@ class System:
         t = C.c_int()
         _ck(lib().sph_system_trim(self.h, C.byref(t)))
         return bool(t.value)
+
+    def diag_many(self, scenes) -> list:
+        """Diagnostics of several scenes in one launch (Scene objects or ids)."""
+        ids = [s.id if isinstance(s, Scene) else int(s) for s in scenes]
+        if not ids:
+            return []
+        arr = (C.c_int * len(ids))(*ids)
+        out = (Diag * len(ids))()
+        _ck(lib().sph_scenes_diag(self.h, len(ids), arr, out))
+        return [d.as_dict() for d in out]
 
     def memory(self) -> int:
         b = C.c_int64()

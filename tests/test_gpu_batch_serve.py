@@ -57,6 +57,36 @@ def test_batched_equals_alone_bitwise():
         assert dg["total_units"] == 0 and rdg["total_units"] == 0
 
 
+def test_diag_many_and_state_fingerprint(tmp_path):
+    """One diagnostic launch over several scenes gives each scene's own
+    diagnostics; the state fingerprint does not depend on where the particles
+    sit in memory (a checkpoint reloaded into another system) and changes
+    with one bit of one particle."""
+    with S.System(tile=128) as sysm:
+        scenes = [sysm.scene_from_request(W.base_params(), r) for r in SMALL[:5]]
+        sysm.step(9)
+        many = sysm.diag_many(scenes[::-1])
+        for sc, d in zip(scenes[::-1], many):
+            assert d == sc.diag()
+        assert len({d["state_hash"] for d in many}) == len(many)
+        scenes[2].save(str(tmp_path / "s2.sphe"))
+        ref = scenes[2].diag()["state_hash"]
+        st = scenes[2].get_particles()
+    with S.System(tile=256) as other:
+        sc = other.scene_from_request(W.base_params(), SMALL[2])
+        sc.load(str(tmp_path / "s2.sphe"))
+        assert sc.diag()["state_hash"] == ref
+        sc.set_particles(st["pos"], st["vel"])  # sediment cleared
+        h0 = sc.diag()["state_hash"]
+        pos = st["pos"].copy()
+        pos[17, 0] = np.nextafter(pos[17, 0], np.float32(1.0))
+        sc.set_particles(pos, st["vel"])
+        assert sc.diag()["state_hash"] != h0
+    with S.System() as sysm:
+        with pytest.raises(S.SphError):
+            sysm.diag_many([12345])
+
+
 def test_step_budgets_retire_scenes_independently():
     with S.System(tile=256) as sysm:
         scenes = [sysm.scene_from_request(W.base_params(), r) for r in SMALL[:4]]
@@ -83,8 +113,8 @@ def test_server_results_same_alone_and_mixed():
         assert res.total_units == 0 and res.nan_particles == 0
         assert res.done_s >= res.admit_s >= res.arrival_s - 1e-6
     # and the same state as stepping the scene directly through a system
-    (st, _) = _alone(SMALL[1], SMALL[1]["steps"])
-    assert mixed[1].state_hash != 0
+    _, dg = _alone(SMALL[1], SMALL[1]["steps"])
+    assert mixed[1].state_hash == dg["state_hash"] != 0
     assert stats["p99_s"] >= stats["p50_s"] > 0
 
 
