@@ -291,7 +291,8 @@ def run_ours(args, spec, config):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + fBm terrain)",
         "config": config,
         "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": NCU_FORCE_TRAFFIC.get((config["workload"], variant, cm)),
+                     "frac": achieved / hbm,
+                     "traffic": NCU_FORCE_TRAFFIC.get((config["workload"], variant & FORCE_BITS, cm)),
                      "peak_kind": kind,
                      "step_bytes_frac": step_bytes / (step_ms * 1e-3) / 1e9 / hbm},
         "issue_roofline": issue_roofline(config["workload"], variant, cm, force_ms, clk.summary()),
@@ -318,15 +319,20 @@ def run_ours(args, spec, config):
 # and its step budget (4 B) that set_params copies to the device.
 C_PARAMS_BYTES = 248 + 4
 
+# The variant bits that select the force kernel (4 register budget, 8 lists,
+# 16 list walk loaded ahead, 128 packed records); the others change only the
+# density pass, whose lists are the same in every variant.
+FORCE_BITS = 4 | 8 | 16 | 128
+
 # DRAM bytes (read + write) of one k_force launch, from an ncu capture of the
 # same workload at the same point of the run (mid-run) with kernel variant 88
-# and cell_mult 0.5 (the neighbour lists the force pass reads are most of
-# it).  Reported only for that configuration.
-NCU_FORCE_TRAFFIC = {("plain_1m", 88, 0.5): 404.4e6}
+# (force bits 24) and cell_mult 0.5 (the neighbour lists the force pass reads
+# are most of it).  Reported only for that force kernel and cell size.
+NCU_FORCE_TRAFFIC = {("plain_1m", 24, 0.5): 404.4e6}
 # Warp instructions of one k_force launch (smsp__inst_executed.sum) from the
 # same capture: with the live kernel time they place the kernel against the
 # instruction-issue roofline (4 warp instructions per cycle per SM).
-NCU_FORCE_WARP_INST = {("plain_1m", 88, 0.5): 397.26e6}
+NCU_FORCE_WARP_INST = {("plain_1m", 24, 0.5): 397.26e6}
 
 
 def issue_roofline(workload, variant, cm, force_ms, clocks):
@@ -334,7 +340,7 @@ def issue_roofline(workload, variant, cm, force_ms, clocks):
     instructions per launch (ncu, same configuration and point of the run)
     over the live CUDA-event time, against 4 per cycle per SM at the
     sampled SM clock."""
-    inst = NCU_FORCE_WARP_INST.get((workload, variant, cm))
+    inst = NCU_FORCE_WARP_INST.get((workload, variant & FORCE_BITS, cm))
     if inst is None or not force_ms:
         return None
     import torch

@@ -119,7 +119,7 @@ typedef struct sph_system_config {
                                      force pass reads them instead of re-testing the
                                      cells; ignored when the HBM budget has no room,
                                 16 = with 8: the force pass's list walk loads ahead,
-                                32 = with 8: middle register budget of the density pass,
+                                32 = with 8: relaxed register budget of the density pass only,
                                 64 = with 8: the density pass loads candidates in pairs,
                                128 = with 8: the force pass gathers one packed 32-byte
                                      record per neighbour (32 more bytes per particle);

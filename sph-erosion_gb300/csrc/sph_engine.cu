@@ -1375,7 +1375,7 @@ void System::autotune(int steps, sph_tune_result* out) {
     };
     const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
-    const int variants[] = {0, 4, 28, 88, 216};
+    const int variants[] = {0, 4, 28, 88, 120, 216};
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;
     float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;

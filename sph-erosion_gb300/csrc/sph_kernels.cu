@@ -1150,8 +1150,8 @@ static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.til
 // (fewer resident blocks, no spills) against the default high occupancy.
 // Bit 3 hands the in-range neighbour lists from the density pass to the force
 // pass (takes precedence over bit 0); bit 4 with it pipelines the force
-// pass's list walk; bit 5 with it gives the density pass a middle register
-// budget (6 resident blocks of 256 threads); bit 6 pairs the density pass's
+// pass's list walk; bit 5 with it relaxes the density pass's register
+// budget alone (4 resident blocks of 256 threads); bit 6 pairs the density pass's
 // candidate loads; bit 7 with bit 3 packs each particle's force-pass inputs
 // into one 32-byte record.
 template <int MINB>
@@ -1173,7 +1173,7 @@ void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
         if (relaxed)
             launch_density_nl<4>(a, s, st);
         else if (s.variant & 32)
-            launch_density_nl<6>(a, s, st);
+            launch_density_nl<4>(a, s, st);
         else
             launch_density_nl<8>(a, s, st);
     } else if (s.variant & 1) {

@@ -140,8 +140,8 @@ def test_autotune_restores_state_and_applies_choice():
         sysm.step(5)
         before = [_state(sc) for sc in scenes]
         tuned = sysm.autotune(4)
-        assert len(tuned["tried"]) == 20 and tuned["tile"] in (128, 256)
-        assert tuned["variant"] in (0, 4, 28, 88, 216)
+        assert len(tuned["tried"]) == 24 and tuned["tile"] in (128, 256)
+        assert tuned["variant"] in (0, 4, 28, 88, 120, 216)
         assert tuned["ms_per_step"] == min(t[3] for t in tuned["tried"])
         for sc, st in zip(scenes, before):
             for a, b in zip(_state(sc), st):
