@@ -141,12 +141,15 @@ def run_reference(args, spec, config):
     import oracle as O
 
     O.build()
+    # each step is a bounded sample of the workload, sized so that the whole
+    # run (warm-up included) takes about 150 s of CPU time at most
+    budget = min(args.ref_seconds, max(0.5, 150.0 / max(args.steps + args.warmup, 1)))
     vals = []
     cores = m = 0
     for _ in range(args.warmup):
-        pass
+        cpu_sample(spec, budget_s=budget)
     for _ in range(args.steps):
-        v, cores, m, _t = cpu_sample(spec, budget_s=args.ref_seconds)
+        v, cores, m, _t = cpu_sample(spec, budget_s=budget)
         vals.append(v)
     val = float(np.median(vals))
     line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "impl": "reference", "n_gpus": args.gpus,
@@ -503,7 +506,7 @@ def main():
     ap.add_argument("--variant", type=int, default=None,
                     help="kernel variant bits of the plain workloads (before autotuning)")
     ap.add_argument("--cell-mult", type=float, default=0.5)
-    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="serving: requests in the trace")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
