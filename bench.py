@@ -43,11 +43,15 @@ def peaks():
 
 
 class Clocks:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    """Samples nvidia-smi clocks and throttle reasons during the timed region.
+    The sampler is started and seen running before the region starts (its
+    start-up takes longer than a short region), and the summary covers the
+    samples from the region's start through the first one after its end."""
 
     def __init__(self):
         self.samples = []
         self.proc = None
+        self.first = 0
 
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -55,10 +59,14 @@ class Clocks:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("LOCAL_RANK", "0"),
-                                          f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                                          f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.samples and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
+            self.first = len(self.samples)
         except Exception:
             self.proc = None
         return self
@@ -71,6 +79,11 @@ class Clocks:
 
     def __exit__(self, *exc):
         if self.proc:
+            end = len(self.samples)
+            t0 = time.perf_counter()
+            while len(self.samples) <= end and time.perf_counter() - t0 < 1.0:
+                time.sleep(0.005)
+            self.samples = self.samples[self.first:]
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
