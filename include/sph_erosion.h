@@ -218,6 +218,10 @@ SPH_API int sph_scene_get_particle(sph_system* s, int scene, int id, sph_particl
 /* All records in id order (SPH_FLAG_RECORD): 27 floats each, laid out as
  * pos3 vel3 acc3 density pressure fpress3 fvisc3 fgrav3 fsurf3 normal3 pad. */
 SPH_API int sph_scene_get_records(sph_system* s, int scene, float* rec27, int* neighb_id);
+/* Diagnostics of a scene (no counterpart in the reference): FP64 momentum and
+ * energies reduced on the device, the int64 sediment and terrain mass units
+ * (their sum is conserved exactly), non-finite positions and the state
+ * fingerprint (sph_diag). */
 SPH_API int sph_scene_diag(sph_system* s, int scene, sph_diag* out);
 /* The same for k scenes in one launch (k <= max_scenes): out[i] for scenes[i]. */
 SPH_API int sph_scenes_diag(sph_system* s, int k, const int* scenes, sph_diag* out);
