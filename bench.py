@@ -424,6 +424,14 @@ def run_batched(args, config):
     sysm.step(args.warmup)
     sysm.sync()
     tuned = sysm.autotune(4) if args.autotune else None
+    if args.kernels_only:
+        sysm.step(args.steps)
+        sysm.sync()
+        sysm.close()
+        for path in paths:
+            os.remove(path)
+        os.rmdir(tmp)
+        return
     with Clocks() as clk:
         ms = barrier_max(sysm.time_steps(args.steps), ws)
     batched = total_all * args.steps / (ms * 1e-3)
@@ -442,6 +450,7 @@ def run_batched(args, config):
             one.step(args.warmup)
             one.sync()
             plain_ms += one.time_steps(args.steps)
+    os.rmdir(tmp)
     plain_ms = barrier_max(plain_ms, ws)
     plain = total_all * args.steps / (plain_ms * 1e-3)
     if rank != 0:
