@@ -336,7 +336,9 @@ typedef struct sph_result {
     int64_t total_units;               /* sediment + terrain change: 0 when mass is conserved */
     int64_t sediment_units;
     int32_t nan_particles;
-    int32_t pad;
+    int32_t status;                    /* 0 when served; an error code (SPH_ERR_CAPACITY) when the
+                                          request was refused at admission: its scene could not be
+                                          created even with nothing else resident */
     double kinetic;
     uint64_t state_hash;               /* sph_diag.state_hash of the final state */
 } sph_result;

@@ -23,11 +23,7 @@
 
 namespace sph {
 
-namespace {
-
 using Clock = std::chrono::steady_clock;
-
-}  // namespace
 
 // Host-side inputs of a request's scene: parameters, particles, terrain.
 struct PreparedScene {
@@ -82,8 +78,10 @@ class Server {
 
     int64_t submit(const sph_request& r, double arrival) {
         if (r.particles <= 0 || r.steps < 0) throw Error(SPH_ERR_INVALID, "request needs particles > 0 and steps >= 0");
-        RecipeGeometry g;
-        recipe_geometry(r, cfg_.base.smoothing_radius, &g);  // validates early
+        // a request whose scene cannot fit even alone (without the optional
+        // neighbour lists) is refused here, not left to block the queue
+        if (request_bytes(r, false) > cfg_.hbm_budget)
+            throw Error(SPH_ERR_CAPACITY, "the request's scene exceeds the whole HBM budget");
         Pending q{next_ticket_++, r, arrival, nullptr, 0};
         queue_.push_back(q);
         return q.ticket;
@@ -156,12 +154,13 @@ class Server {
         return s;
     }
 
-    int64_t request_bytes(const sph_request& r) {
+    // Device bytes of a request's scene (validates the request's geometry).
+    int64_t request_bytes(const sph_request& r, bool lists = true) {
         RecipeGeometry g;
         recipe_geometry(r, cfg_.base.smoothing_radius, &g);
         sph_params p;
         recipe_params(cfg_.base, g, &p);
-        return sys_.scene_bytes(r.particles, r.terrain_side, r.terrain_side, p);
+        return sys_.scene_bytes(r.particles, r.terrain_side, r.terrain_side, p, lists);
     }
 
     void admit() {
@@ -173,8 +172,10 @@ class Server {
             const auto it = ready_.begin();
             Pending& q = it->second;
             const int64_t need = request_bytes(q.req);
-            if (need > cfg_.hbm_budget) throw Error(SPH_ERR_CAPACITY, "a request exceeds the whole HBM budget");
-            if (reserved_ + need > cfg_.hbm_budget) break;
+            // with nothing resident a request is admitted even when its
+            // lists do not fit (submit made sure the rest does): it then
+            // runs without them
+            if (reserved_ + need > cfg_.hbm_budget && !active_.empty()) break;
             if (cfg_.max_active_particles > 0 && !active_.empty() &&
                 resident_particles_ + q.req.particles > cfg_.max_active_particles)
                 break;
@@ -189,7 +190,8 @@ class Server {
                         trimmed = true;
                         continue;
                     }
-                    throw;
+                    refuse(it, e.code);  // cannot fit even alone: retire it with its error
+                    continue;
                 }
                 throw;
             }
@@ -205,6 +207,23 @@ class Server {
             stats_.peak_bytes = std::max<int64_t>(stats_.peak_bytes, sys_.memory_bytes());
             if (retire_next) break;  // retire it on the next round
         }
+    }
+
+    // Retire a request without running it: its result carries the error.
+    void refuse(std::multimap<double, Pending>::iterator it, int code) {
+        const Pending& q = it->second;
+        sph_result r;
+        std::memset(&r, 0, sizeof r);
+        r.ticket = q.ticket;
+        r.seed = q.req.seed;
+        r.particles = q.req.particles;
+        r.steps = q.req.steps;
+        r.arrival_s = q.arrival;
+        r.admit_s = r.done_s = now();
+        r.status = code;
+        prepared_bytes_ -= q.held;
+        done_.push_back(r);
+        ready_.erase(it);
     }
 
     // Move the requests that have arrived by time t into the ready set,
@@ -448,6 +467,7 @@ SPH_API int sph_server_run_trace(sph_server* s, const sph_request* reqs, int n, 
         std::vector<double> lat;
         double first = 1e300, last = 0.0;
         for (const sph_result& r : d) {
+            if (r.status != 0) continue;  // refused: not served
             lat.push_back(r.done_s - r.arrival_s);
             first = std::min(first, r.arrival_s);
             last = std::max(last, r.done_s);

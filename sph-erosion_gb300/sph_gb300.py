@@ -78,7 +78,7 @@ class Result(C.Structure):
     _fields_ = [("ticket", C.c_int64), ("seed", C.c_uint64), ("particles", C.c_int32), ("steps", C.c_int32),
                 ("arrival_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
                 ("total_units", C.c_int64), ("sediment_units", C.c_int64), ("nan_particles", C.c_int32),
-                ("pad", C.c_int32), ("kinetic", C.c_double), ("state_hash", C.c_uint64)]
+                ("status", C.c_int32), ("kinetic", C.c_double), ("state_hash", C.c_uint64)]
 
 
 class ServerStats(C.Structure):

@@ -108,3 +108,17 @@ def test_grid_beyond_key_limit_is_refused():
         assert e.value.code == -4
         sc = sysm.scene(S.default_params(**dict(W.PHYS, box_half=(10.0, 1.0, 10.0), cell_mult=1.0)))
         assert sc.grid_dims()[3] <= (1 << 30) + 1
+
+
+def test_server_refuses_a_request_that_cannot_fit():
+    """A request whose scene exceeds the whole HBM budget is refused when it
+    is submitted, so it cannot block the queue; the server goes on serving."""
+    small = dict(seed=7001, particles=2048, terrain_side=64, steps=12)
+    big = dict(seed=7002, particles=262144, terrain_side=512, steps=12)
+    with S.Server(W.base_params(), chunk_steps=8, hbm_budget=24 << 20) as srv:
+        with pytest.raises(S.SphError) as e:
+            srv.submit(big)
+        assert e.value.code == -4
+        (res,), stats = srv.run_trace([dict(small, arrival_s=0.0)])
+    assert stats["completed"] == 1
+    assert res.status == 0 and res.total_units == 0 and res.state_hash != 0
