@@ -112,3 +112,31 @@ def test_frame_loop_example_compiles_as_c_and_links(built_lib, tmp_path):
     r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", f"-I{ROOT}/include", str(src), "-o", str(exe),
                         f"-L{PKG}", "-lsph_gb300", f"-Wl,-rpath,{PKG}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    """Every public struct's size and field offsets, as the C compiler lays
+    them out from include/sph_erosion.h, equal the Python binding's ctypes
+    mirrors."""
+    import sph_gb300 as S
+
+    pairs = {"sph_params": S.Params, "sph_particle": S.Particle, "sph_diag": S.Diag,
+             "sph_system_config": S.SystemConfig, "sph_tune_result": S.TuneResult, "sph_request": S.Request,
+             "sph_server_config": S.ServerConfig, "sph_result": S.Result, "sph_server_stats": S.ServerStats}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "sph_erosion.h"', "int main(void) {"]
+    want = []
+    for cname, cls in pairs.items():
+        lines.append(f'    printf("%zu\\n", sizeof({cname}));')
+        want.append(C.sizeof(cls))
+        for fname, *_ in cls._fields_:
+            lines.append(f'    printf("%zu\\n", offsetof({cname}, {fname}));')
+            want.append(getattr(cls, fname).offset)
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", f"-I{ROOT}/include", str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want
