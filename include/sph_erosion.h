@@ -355,14 +355,17 @@ typedef struct sph_server_stats {
     int64_t peak_particles;  /* most particles resident at once */
     /* host wall time by phase of the serving loop (seconds): admission
      * (scene uploads), preparing queued requests' inputs while a chunk runs
-     * on the GPU, waiting for the chunk, retirement (readback, checks) */
+     * on the GPU, waiting for the chunk, retirement (one diagnostic launch
+     * for the finished scenes, then their ranges are freed) */
     double admit_s, prepare_s, gpu_wait_s, retire_s;
 } sph_server_stats;
 
 SPH_API void sph_server_config_default(sph_server_config* c);
 SPH_API int sph_server_create(const sph_server_config* cfg, sph_server** out);
 SPH_API int sph_server_destroy(sph_server* s);
-/* Queue a request (its arrival_s is ignored: it arrives now). */
+/* Queue a request (its arrival_s is ignored: it arrives now).  A request
+ * whose scene cannot fit the budget even alone is refused here with
+ * SPH_ERR_CAPACITY. */
 SPH_API int sph_server_submit(sph_server* s, const sph_request* r, int64_t* ticket);
 /* Admit what fits, run one chunk of batched steps, retire finished scenes
  * and copy up to `cap` completed results out; *n_out = number copied,

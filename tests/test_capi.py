@@ -114,6 +114,45 @@ def test_frame_loop_example_compiles_as_c_and_links(built_lib, tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+SERVER_LOOP_C = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "sph_erosion.h"
+static void report(const char* msg) { fprintf(stderr, "%s\n", msg); }
+static void deliver(const sph_result* r) { (void)r; }
+int serve_one(void) {
+    sph_server_config scfg; sph_server_config_default(&scfg);
+    scfg.hbm_budget = (int64_t)120 << 30;
+    scfg.policy = 1;
+    sph_server* srv; if (sph_server_create(&scfg, &srv) != SPH_OK) return 1;
+    sph_request r = {0};
+    r.seed = 42; r.particles = 65536; r.terrain_side = 256; r.steps = 500;
+    int64_t ticket;
+    if (sph_server_submit(srv, &r, &ticket) != SPH_OK)
+        report(sph_last_error());
+    sph_result out[64]; int n, active;
+    do {
+        sph_server_poll(srv, out, 64, &n, &active);
+        for (int i = 0; i < n; ++i)
+            if (out[i].status == SPH_OK) deliver(&out[i]);
+    } while (active > 0);
+    return sph_server_destroy(srv);
+}
+int main(void) { return 0; }  /* linked, not run: serving needs a GPU */
+"""
+
+
+def test_server_example_compiles_as_c_and_links(built_lib, tmp_path):
+    """The serving loop shown for C callers compiles as C99 against the
+    header and links against the library."""
+    src = tmp_path / "serve.c"
+    src.write_text(SERVER_LOOP_C)
+    exe = tmp_path / "serve"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", f"-I{ROOT}/include", str(src), "-o", str(exe),
+                        f"-L{PKG}", "-lsph_gb300", f"-Wl,-rpath,{PKG}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_ctypes_mirrors_match_the_header_layout(tmp_path):
     """Every public struct's size and field offsets, as the C compiler lays
     them out from include/sph_erosion.h, equal the Python binding's ctypes
