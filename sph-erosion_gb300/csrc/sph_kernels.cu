@@ -1,6 +1,8 @@
 // Hand-written sm_103a kernels of one simulation step, all scenes of a system
-// per launch.  Persistent grid-stride loops over a work list of tiles; a scene
-// whose step budget is exhausted is skipped.
+// per launch.  Each kernel walks a work list of (scene, tile) items in a
+// grid-stride loop; the particle passes are launched with one block per tile,
+// so the hardware hands tiles to SMs as they free up.  A scene whose step
+// budget is exhausted is skipped.
 //
 // Stage order per step (the reference's Run, Erosion/fluid_system.h:104-183,
 // with its three O(N^2) passes replaced by a uniform grid):
