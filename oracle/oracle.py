@@ -96,6 +96,11 @@ def lib():
         L.oracle_run_f32x.argtypes = L.oracle_run_f32.argtypes
         L.oracle_run_f64.argtypes = [C.POINTER(OracleParams), C.c_int, f64p, f64p, i32p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        for nm, fp in (("oracle_sample_f32", f32p), ("oracle_sample_f32x", f32p), ("oracle_sample_f64", f64p)):
+            fn = getattr(L, nm)
+            fn.argtypes = [C.POINTER(OracleParams), C.c_int, fp, fp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                           i32p, fp, fp, fp, i32p, i32p, i32p, i32p, C.c_int]
+            fn.restype = C.c_int
         L.oracle_time_sample.argtypes = [C.POINTER(OracleParams), C.c_int, f32p, f32p, C.c_int, C.c_int,
                                          C.c_int]
         L.oracle_time_sample.restype = C.c_double
@@ -139,6 +144,67 @@ def run(params: OracleParams, pos, vel=None, nsteps=1, nbid=None, sed=None, base
     fn = {"f32": lib().oracle_run_f32, "f32x": lib().oracle_run_f32x, "f64": lib().oracle_run_f64}[precision]
     fn(C.byref(params), n, pos, vel, nbid, _ptr(sed), _ptr(base), _ptr(delta), _ptr(rec), int(nsteps),
        int(nthreads))
+    return dict(pos=pos, vel=vel, nbid=nbid, sed=sed, delta=delta, rec=rec)
+
+
+def sample(params: OracleParams, pos, vel, ids, sed=None, base=None, delta=None, nbid=None, precision="f32",
+           nthreads=0):
+    """One step of the particles `ids` from the state of all of them: the
+    values oracle_run computes for those particles, with each neighbour sum
+    over the in-range set in ascending index (found through a grid, so large
+    scenes are cheap).  Returns a dict with rec, pos, vel, nbid, sed, q and
+    qv of the sample, in the order of `ids`."""
+    dt = np.float64 if precision == "f64" else np.float32
+    n = len(pos)
+    pos = np.ascontiguousarray(np.asarray(pos, dt).reshape(n, 3))
+    vel = np.ascontiguousarray(np.asarray(vel, dt).reshape(n, 3))
+    ids = np.ascontiguousarray(ids, np.int32)
+    m = len(ids)
+    if m and (ids.min() < 0 or ids.max() >= n):
+        raise ValueError("sample ids out of range")
+    sed = None if sed is None else np.ascontiguousarray(sed, np.int32)
+    ntex = params.tw * params.td if params.terrain else 0
+    base = np.zeros(max(ntex, 1), np.float32) if base is None else np.ascontiguousarray(base, np.float32).ravel()
+    delta = np.zeros(max(ntex, 1), np.int64) if delta is None else np.ascontiguousarray(delta, np.int64).ravel()
+    if ntex and (base.size < ntex or delta.size < ntex):
+        raise ValueError("terrain arrays smaller than tw * td")
+    out = dict(rec=np.zeros((m, REC), dt), pos=np.zeros((m, 3), dt), vel=np.zeros((m, 3), dt),
+               nbid=(np.full(m, -1, np.int32) if nbid is None else np.ascontiguousarray(nbid, np.int32)[ids].copy()),
+               sed=np.zeros(m, np.int32), q=np.zeros(m, np.int32), qv=np.zeros(m, np.int32))
+    fn = {"f32": lib().oracle_sample_f32, "f32x": lib().oracle_sample_f32x, "f64": lib().oracle_sample_f64}[precision]
+    rc = fn(C.byref(params), n, pos, vel, _ptr(sed), _ptr(base), _ptr(delta), m, ids, out["rec"], out["pos"],
+            out["vel"], out["nbid"], out["sed"], out["q"], out["qv"], int(nthreads))
+    if rc != 0:
+        raise RuntimeError("oracle sample: an in-range set exceeds 4096 particles")
+    return out
+
+
+def run_grid(params: OracleParams, pos, vel=None, nsteps=1, nbid=None, sed=None, base=None, delta=None,
+             precision="f32", nthreads=0):
+    """oracle.run's result (same arithmetic, same sums, bit for bit) for
+    larger scenes: each step is oracle.sample over every particle, whose
+    neighbour sums run over the in-range sets found through a grid instead
+    of all pairs.  Returns the same dict as run (rec of the last step)."""
+    dt = np.float64 if precision == "f64" else np.float32
+    n = len(pos)
+    pos = np.ascontiguousarray(np.asarray(pos, dt).reshape(n, 3)).copy()
+    vel = np.zeros((n, 3), dt) if vel is None else np.ascontiguousarray(np.asarray(vel, dt).reshape(n, 3)).copy()
+    nbid = np.full(n, -1, np.int32) if nbid is None else np.ascontiguousarray(nbid, np.int32).copy()
+    sed = np.zeros(n, np.int32) if sed is None else np.ascontiguousarray(sed, np.int32).copy()
+    ntex = params.tw * params.td if params.terrain else 0
+    base = np.zeros(max(ntex, 1), np.float32) if base is None else np.ascontiguousarray(base, np.float32).ravel()
+    delta = (np.zeros(max(ntex, 1), np.int64) if delta is None
+             else np.ascontiguousarray(delta, np.int64).ravel().copy())
+    ids = np.arange(n, dtype=np.int32)
+    rec = None
+    for _ in range(int(nsteps)):
+        s = sample(params, pos, vel, ids, sed=sed, base=base, delta=delta, nbid=nbid, precision=precision,
+                   nthreads=nthreads)
+        pos, vel, nbid, rec = s["pos"], s["vel"], s["nbid"], s["rec"]
+        if params.terrain and params.erosion:
+            sed = s["sed"]
+            m = s["qv"] >= 0
+            np.subtract.at(delta, s["qv"][m], s["q"][m].astype(np.int64))
     return dict(pos=pos, vel=vel, nbid=nbid, sed=sed, delta=delta, rec=rec)
 
 

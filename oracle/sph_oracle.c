@@ -89,6 +89,33 @@ void oracle_run_f64(const oracle_params* p, int n, double* pos, double* vel, int
     f64_run(p, n, pos, vel, nbid, sed, base, delta, rec, nsteps);
 }
 
+int oracle_sample_f32(const oracle_params* p, int n, const float* pos, const float* vel, const int32_t* sed,
+                      const float* base, const int64_t* delta, int m, const int* ids, float* rec, float* pos_out,
+                      float* vel_out, int* nbid_inout, int32_t* sed_out, int32_t* q_out, int* qv_out,
+                      int nthreads) {
+    set_threads(nthreads);
+    return f32_sample(p, n, pos, vel, sed, base, delta, m, ids, rec, pos_out, vel_out, nbid_inout, sed_out, q_out,
+                      qv_out);
+}
+
+int oracle_sample_f32x(const oracle_params* p, int n, const float* pos, const float* vel, const int32_t* sed,
+                       const float* base, const int64_t* delta, int m, const int* ids, float* rec, float* pos_out,
+                       float* vel_out, int* nbid_inout, int32_t* sed_out, int32_t* q_out, int* qv_out,
+                       int nthreads) {
+    set_threads(nthreads);
+    return f32x_sample(p, n, pos, vel, sed, base, delta, m, ids, rec, pos_out, vel_out, nbid_inout, sed_out, q_out,
+                       qv_out);
+}
+
+int oracle_sample_f64(const oracle_params* p, int n, const double* pos, const double* vel, const int32_t* sed,
+                      const float* base, const int64_t* delta, int m, const int* ids, double* rec, double* pos_out,
+                      double* vel_out, int* nbid_inout, int32_t* sed_out, int32_t* q_out, int* qv_out,
+                      int nthreads) {
+    set_threads(nthreads);
+    return f64_sample(p, n, pos, vel, sed, base, delta, m, ids, rec, pos_out, vel_out, nbid_inout, sed_out, q_out,
+                      qv_out);
+}
+
 /* ---- CPU-baseline timing sample ------------------------------------------ */
 double oracle_time_sample(const oracle_params* p, int n, const float* pos, const float* vel, int i0, int m,
                           int nthreads) {

@@ -66,6 +66,28 @@ void oracle_run_f32x(const oracle_params* p, int n, float* pos, float* vel, int*
 void oracle_run_f64(const oracle_params* p, int n, double* pos, double* vel, int* nbid, int32_t* sed,
                     const float* base, int64_t* delta, double* rec, int nsteps, int nthreads);
 
+/* One step of the particles ids[0..m) only, from the state of all n (pos,
+ * vel: 3n; sed: n units, may be null; base/delta: the terrain).  Each
+ * neighbour sum runs over the particle's in-range set in ascending index,
+ * found through a uniform grid, which is term for term the all-pairs sum of
+ * oracle_run_*: the results equal what oracle_run_* computes for those
+ * particles.  Per sample: rec (ORACLE_REC floats), next pos and vel (3
+ * each), NeighbId (nbid_inout: in = the state's, out = the step's), sediment,
+ * units moved from the terrain (q) and their vertex (qv, -1 when none).  Any
+ * output may be null.  Returns 0, or -1 if an in-range set exceeds 4096. */
+int oracle_sample_f32(const oracle_params* p, int n, const float* pos, const float* vel, const int32_t* sed,
+                      const float* base, const int64_t* delta, int m, const int* ids, float* rec, float* pos_out,
+                      float* vel_out, int* nbid_inout, int32_t* sed_out, int32_t* q_out, int* qv_out,
+                      int nthreads);
+int oracle_sample_f32x(const oracle_params* p, int n, const float* pos, const float* vel, const int32_t* sed,
+                       const float* base, const int64_t* delta, int m, const int* ids, float* rec, float* pos_out,
+                       float* vel_out, int* nbid_inout, int32_t* sed_out, int32_t* q_out, int* qv_out,
+                       int nthreads);
+int oracle_sample_f64(const oracle_params* p, int n, const double* pos, const double* vel, const int32_t* sed,
+                      const float* base, const int64_t* delta, int m, const int* ids, double* rec, double* pos_out,
+                      double* vel_out, int* nbid_inout, int32_t* sed_out, int32_t* q_out, int* qv_out,
+                      int nthreads);
+
 /* Timing sample for the CPU baseline: the reference's three all-pairs passes
  * and the integration for particles [i0, i0+m) against all n particles
  * (densities of the other particles are taken as p0).  Writes nothing back. */

@@ -889,6 +889,7 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
                 py = ts.y;
             }
         }
+        bool moved = false;
         {
             float cp[3], nr[3];
             if (box_collide(S, px, py, pz, cp, nr) && dt != 0.0f) {
@@ -898,6 +899,7 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
                 vx = fs(vx, fm(fm(nr[0], f), vdn));
                 vy = fs(vy, fm(fm(nr[1], f), vdn));
                 vz = fs(vz, fm(fm(nr[2], f), vdn));
+                moved = px != cp[0] || pz != cp[2];
                 px = cp[0];
                 py = cp[1];
                 pz = cp[2];
@@ -905,6 +907,10 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
         }
         int sed = __float_as_int(vi.w);
         if (has_t && (S.flags & kFlagErosion)) {
+            // the exchange uses the surface under the particle's final
+            // position: a wall that moved it in x or z moved it to another
+            // sample of the terrain
+            if (moved) ts = terrain_at(S, a.theight, px, pz);
             const float e = fs(py, ts.y);
             if (e <= S.layer) {
                 float capf = fm(S.k_capacity, len3(vx, vy, vz));

@@ -51,12 +51,22 @@ def run_ref(params, pos, steps, vel=None):
 
 
 def fp64_fixture():
-    """FP64 oracle state of the 16,384-particle block after 100 steps (rounded
-    to float32), the yardstick of the reference's own rounding error."""
+    """FP64 oracle records of the 16,384-particle block after 100 steps
+    (rounded to float32), the yardstick of the reference's own rounding
+    error."""
     spec = W.plain_small(erosion=False, terrain=False)
     p = O.make_params(box_l=(0.5, 0.5, 0.5), **{k: v for k, v in C1_REF.items() if k != "len"})
     out = O.run(p, spec["pos"], nsteps=100, precision="f64")
-    save("fp64_c1_16384.npz", state100=out["rec"][:, 0:11].astype(np.float32))
+    save("fp64_c1_16384.npz", rec100=out["rec"].astype(np.float32))
+
+
+def c1_16384_fixture():
+    """The full 16,384-particle plain-small block (32 x 16 x 32), no terrain
+    (the reference has none): records after 1 and after 100 steps."""
+    spec = W.plain_small(erosion=False, terrain=False)
+    res = run_ref(C1_REF, spec["pos"], [1, 100])
+    save("ref_c1_16384.npz", pos0=spec["pos"], rec1=res[1][0], nb1=res[1][1], cnt1=res[1][2].astype(np.int16),
+         rec100=res[100][0], nb100=res[100][1], cnt100=res[100][2].astype(np.int16))
 
 
 def collision_fixture():
@@ -122,12 +132,8 @@ def main(ref_root):
     save("ref_c1_2048.npz", pos0=pos, rec1=res[1][0], nb1=res[1][1], cnt1=res[1][2].astype(np.int16),
          rec100=res[100][0], nb100=res[100][1], cnt100=res[100][2].astype(np.int16))
 
-    # 3. The full 16,384-particle plain-small block (32 x 16 x 32), no terrain:
-    #    full records after 1 step, state after 100 steps.
-    spec = W.plain_small(erosion=False, terrain=False)
-    res = run_ref(C1_REF, spec["pos"], [1, 100])
-    save("ref_c1_16384.npz", pos0=spec["pos"], rec1=res[1][0], nb1=res[1][1], cnt1=res[1][2].astype(np.int16),
-         state100=res[100][0][:, 0:11], nb100=res[100][1], cnt100=res[100][2].astype(np.int16))
+    # 3. The full 16,384-particle plain-small block.
+    c1_16384_fixture()
 
     # 4. Edge cases: coincident particles (AddParticles at the same origin,
     #    fluid_system.h:232-251), a lone particle in free fall, particles
@@ -173,6 +179,11 @@ def main(ref_root):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if "--c1-16384-only" in sys.argv:
+        O.build_ref(args[0] if args else "/root/reference")
+        c1_16384_fixture()
+        fp64_fixture()
+        sys.exit(0)
     if "--collision-only" in sys.argv:
         O.build_ref(args[0] if args else "/root/reference")
         collision_fixture()

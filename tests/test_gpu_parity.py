@@ -79,9 +79,6 @@ def test_plain_2048_parity(oracle_lib, golden, ordered):
     assert max(e1.values()) <= RTOL
     assert np.array_equal(nb1, g["nb1"])
     rec, nb = out[100]
-    if ordered:
-        x = O.run(p, g["pos0"], nsteps=100, precision="f32x")
-        assert np.array_equal(rec, x["rec"]) and np.array_equal(nb, x["nbid"])
     f64 = O.run(p, g["pos0"], nsteps=100, precision="f64")["rec"]
     e_ref = field_errors(rec, g["rec100"])
     e_gpu64 = field_errors(rec, f64)
@@ -89,15 +86,35 @@ def test_plain_2048_parity(oracle_lib, golden, ordered):
     _report(f"2048 ordered={ordered} step 100 vs reference", e_ref)
     _report(f"2048 ordered={ordered} step 100 gpu vs fp64", e_gpu64)
     _report("2048 step 100 reference vs fp64", e_ref64)
-    for k in ("pos", "density"):
-        assert e_ref[k] <= RTOL, k
+    if ordered:
+        # equal to the f32x oracle, so the distance to the reference is the
+        # powf residual alone: every field within RTOL except the ones in
+        # POWF_RESIDUAL_2048, which equal that residual exactly
+        x = O.run(p, g["pos0"], nsteps=100, precision="f32x")
+        assert np.array_equal(rec, x["rec"]) and np.array_equal(nb, x["nbid"])
+        assert e_ref == field_errors(x["rec"], g["rec100"])
+        for k, v in e_ref.items():
+            assert v <= POWF_RESIDUAL_2048.get(k, RTOL), (k, v)
+    else:
+        for k in ("pos", "density"):
+            assert e_ref[k] <= RTOL, k
     for k in e_gpu64:
         assert e_gpu64[k] <= ENVELOPE * e_ref64[k] + 1e-6, k
 
 
+# Where the f32x oracle (the reference's arithmetic with correctly rounded
+# x^2 and x^3) is more than RTOL from the reference after 100 steps of the
+# 2,048-particle block: glibc's powf(x, 3.0f) rounds differently from the
+# correctly rounded cube on about 0.07% of inputs (powf(x, 2.0f) never
+# does), and 100 steps of the flow amplify those last-bit differences.
+# Measured on the CPU: f32x vs reference, acceleration 1.353e-4, pressure
+# force 1.242e-4 (every other field below 1e-4).
+POWF_RESIDUAL_2048 = {"acc": 1.36e-4, "fpress": 1.25e-4}
+
+
 def test_plain_16384_parity(golden):
     g = golden("ref_c1_16384.npz")
-    f64 = golden("fp64_c1_16384.npz")["state100"]
+    f64 = golden("fp64_c1_16384.npz")["rec100"]
     out = run(C1, g["pos0"], [1, 100])
     rec, nb = out[1]
     errs = field_errors(rec, g["rec1"])
@@ -105,22 +122,15 @@ def test_plain_16384_parity(golden):
     assert max(errs.values()) <= RTOL
     assert np.array_equal(nb, g["nb1"])
     rec, _ = out[100]
-    st = g["state100"]
-    parts = {"pos": slice(0, 3), "vel": slice(3, 6), "acc": slice(6, 9), "density": slice(9, 10),
-             "pressure": slice(10, 11)}
-
-    def err(a, b, sl):
-        return float(np.abs(a[:, sl].astype(np.float64) - b[:, sl]).max() / np.abs(b[:, sl]).max())
-
-    e_ref = {k: err(rec, st, sl) for k, sl in parts.items()}
-    e_gpu64 = {k: err(rec, f64, sl) for k, sl in parts.items()}
-    e_ref64 = {k: err(st, f64, sl) for k, sl in parts.items()}
+    e_ref = field_errors(rec, g["rec100"])
+    e_gpu64 = field_errors(rec, f64)
+    e_ref64 = field_errors(g["rec100"], f64)
     _report("16384 step 100 vs reference", e_ref)
     _report("16384 step 100 gpu vs fp64", e_gpu64)
     _report("16384 step 100 reference vs fp64", e_ref64)
     for k in ("pos", "density"):
         assert e_ref[k] <= RTOL, k
-    for k in parts:
+    for k in e_gpu64:
         assert e_gpu64[k] <= ENVELOPE * e_ref64[k] + 1e-6, k
 
 
@@ -148,7 +158,7 @@ def test_neighbour_counts_bit_exact(oracle_lib, golden, name, key, h):
 def test_keys_and_sorted_order_bit_exact(golden, oracle_lib, cell_mult):
     O = oracle_lib
     g = golden("ref_c1_16384.npz")
-    pos = g["state100"][:, 0:3]
+    pos = g["rec100"][:, 0:3]
     with S.System(particle_capacity=len(pos)) as sysm:
         sc = sysm.scene(S.default_params(**C1, cell_mult=cell_mult))
         sc.set_particles(pos)

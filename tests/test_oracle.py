@@ -158,7 +158,7 @@ def test_keys_and_stable_order(oracle_lib, golden):
     g = golden("ref_c1_16384.npz")
     p = O.make_params(box_l=(0.5, 0.5, 0.5), **C1)
     grd = O.grid(p, 1.0)
-    pos = g["state100"][:, 0:3]
+    pos = g["rec100"][:, 0:3]
     keys = O.cell_keys(grd, pos)
     assert keys.max() < grd.nkeys - 1
     perm = O.stable_sort(keys, grd.nkeys)
@@ -223,3 +223,91 @@ def test_reference_harness_matches_when_present(oracle_lib):
     rec, _, nb = R.get()
     out = O.run(ref_params(O), pos, nsteps=3)
     assert np.array_equal(out["rec"], rec) and np.array_equal(out["nbid"], nb)
+
+
+# ---- the sampled step equals the all-pairs step --------------------------------
+
+def _erosion_case(O, n=900, wall=False):
+    import workloads as W
+
+    bh = (0.25, 0.25, 0.25)
+    pos = W.scaled_block(n, box_half=bh, amp=0.05)
+    tw, td = 24, 20
+    base = O.fbm(5, tw, td, 3, 0.05).ravel()
+    prm = O.make_params(box_l=bh, terrain=(tw, td), height_unit=1e-6, erosion=True, k_capacity=0.05,
+                        k_pickup=5.0, k_deposit=2.0, layer=0.04, **C1)
+    vel = np.zeros_like(pos)
+    vel[:, 0] = -3.0 if wall else 1.5
+    vel[:, 1] = -0.5
+    return prm, pos, vel, base
+
+
+@pytest.mark.parametrize("precision", ["f32", "f32x", "f64"])
+def test_sample_equals_all_pairs(oracle_lib, golden, precision):
+    """oracle.sample on every particle (shuffled order) reproduces
+    oracle.run's one step bit for bit: records, next state, NeighbId."""
+    O = oracle_lib
+    g = golden("ref_c1_2048.npz")
+    p = O.make_params(box_l=(0.5, 0.5, 0.5), **C1)
+    st = O.run(p, g["pos0"], nsteps=60, precision=precision)  # a moving state
+    nxt = O.run(p, st["pos"], st["vel"], nsteps=1, nbid=st["nbid"], precision=precision)
+    ids = np.random.default_rng(1).permutation(len(st["pos"])).astype(np.int32)
+    s = O.sample(p, st["pos"], st["vel"], ids, nbid=st["nbid"], precision=precision)
+    assert np.array_equal(s["rec"], nxt["rec"][ids])
+    assert np.array_equal(s["pos"], nxt["pos"][ids]) and np.array_equal(s["vel"], nxt["vel"][ids])
+    assert np.array_equal(s["nbid"], nxt["nbid"][ids])
+
+
+@pytest.mark.parametrize("wall", [False, True])
+def test_sample_equals_all_pairs_with_erosion(oracle_lib, wall):
+    """The same with terrain contact and the erosion exchange: sediment of
+    each particle, and the units and vertex of each exchange, whose sum is
+    the all-pairs run's terrain delta."""
+    O = oracle_lib
+    prm, pos, vel, base = _erosion_case(O, wall=wall)
+    st = O.run(prm, pos, vel, nsteps=12, base=base, precision="f32x")
+    nxt = O.run(prm, st["pos"], st["vel"], nsteps=1, nbid=st["nbid"], sed=st["sed"], base=base,
+                delta=st["delta"], precision="f32x")
+    ids = np.arange(len(pos), dtype=np.int32)
+    s = O.sample(prm, st["pos"], st["vel"], ids, sed=st["sed"], base=base, delta=st["delta"], nbid=st["nbid"],
+                 precision="f32x")
+    assert np.array_equal(s["rec"], nxt["rec"]) and np.array_equal(s["sed"], nxt["sed"])
+    d = st["delta"].copy()
+    np.subtract.at(d, s["qv"][s["qv"] >= 0], s["q"][s["qv"] >= 0].astype(np.int64))
+    assert np.array_equal(d, nxt["delta"])
+    assert (s["q"] != 0).any()
+
+
+def test_erosion_samples_the_terrain_under_the_final_position(oracle_lib):
+    """A particle that the box wall moves back along x exchanges sediment
+    with the vertex under its clamped position, not the one under the
+    position before the wall."""
+    O = oracle_lib
+    prm, pos, vel, base = _erosion_case(O, wall=True)
+    tw, td = prm.tw, prm.td
+    # one particle just inside the x = -0.25 wall, in the erosion layer,
+    # moving fast enough to cross the wall within the step
+    x = np.array([[-0.245, -0.25 + 0.055, 0.01]], np.float32)
+    v = np.array([[-8.0, 0.0, 0.0]], np.float32)
+    out = O.sample(prm, x, v, np.array([0], np.int32), sed=np.zeros(1, np.int32), base=base,
+                   delta=np.zeros(tw * td, np.int64), precision="f32")
+    assert out["pos"][0, 0] == np.float32(-0.25)
+    assert out["q"][0] > 0
+    # the nearest vertex of the final (clamped) position
+    f32 = np.float32
+    isx = f32(1.0) / f32(f32(0.5) / f32(tw - 1))
+    isz = f32(1.0) / f32(f32(0.5) / f32(td - 1))
+    fx = max(f32(0.0), f32(f32(out["pos"][0, 0] - f32(-0.25)) * isx))
+    fz = max(f32(0.0), f32(f32(out["pos"][0, 2] - f32(-0.25)) * isz))
+    assert out["qv"][0] == int(f32(fz + f32(0.5))) * tw + int(f32(fx + f32(0.5)))
+
+
+def test_run_grid_equals_run(oracle_lib):
+    """Several grid-driven steps equal the all-pairs run bit for bit, with
+    terrain and erosion (sediment and terrain deltas included)."""
+    O = oracle_lib
+    prm, pos, vel, base = _erosion_case(O)
+    a = O.run(prm, pos, vel, nsteps=15, base=base, precision="f32")
+    b = O.run_grid(prm, pos, vel, nsteps=15, base=base, precision="f32")
+    for k in ("pos", "vel", "nbid", "sed", "delta", "rec"):
+        assert np.array_equal(a[k], b[k]), k
