@@ -9,15 +9,26 @@ terrain (see sph-erosion_gb300/workloads.py).  `value` is particle-steps/s
 with the state resident in HBM, each timed step bracketed by CUDA events on
 the library's stream and preceded by an L2 flush; `e2e` is the same metric
 through the C ABI with a parameter upload and a positions readback to host
-memory inside every timed step.  `--impl reference` times the reference's
-algorithm (the oracle's FP32 restatement of FluidSystemSPH::Run, all-pairs)
-on the host cores over a bounded sample of the same workload.
+memory inside every timed step.  The same line carries, measured in the same
+run, the batched form (256 seeded scenes in one system against each scene in
+a system of its own) and the served form (a seeded Poisson request trace
+through the continuous-batching server, with p50/p99 latency).
+`--impl reference` times the reference's algorithm (the oracle's FP32
+restatement of FluidSystemSPH::Run, all-pairs) on the host cores over a
+bounded sample of the same workload.
+
+With --gpus N > 1 and no launcher around it, bench.py starts N ranks itself
+(torch.distributed.run, one process per GPU); the plain scene runs as
+replicas, batched scenes and served requests shard across the ranks.
 """
 from __future__ import annotations
 
 import argparse
+import csv
+import hashlib
 import json
 import os
+import socket
 import subprocess
 import sys
 import tempfile
@@ -40,6 +51,107 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def port_calibration():
+    """How fast the oracle's FP32 port runs against the reference's own
+    FluidSystemSPH::Run on the same host (oracle/port_calibration.json,
+    written by oracle/calibrate.py where the reference sources exist): the
+    CPU baseline times the port, which is the faster of the two, so the
+    reported baseline flatters the reference by this factor."""
+    try:
+        with open(os.path.join(ROOT, "oracle", "port_calibration.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+COUNTERS = os.path.join(ROOT, "profiles", "counters_k_force.json")
+KERNEL_SOURCES = ("sph_kernels.cu", "sph_kernels.h", "sph_types.h")
+
+
+def source_digest() -> str:
+    """Digest of the kernels' source files: counters captured from another
+    build of the kernels are not reported as this build's."""
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "sph-erosion_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+# The variant bits that select the force kernel (4 register budget, 8 lists,
+# 16 list walk loaded ahead, 128 packed records); the others change only the
+# density pass, whose lists are the same in every variant.
+FORCE_BITS = 4 | 8 | 16 | 128
+
+
+def ncu_counters(workload, variant, cm):
+    """The force kernel's DRAM bytes and warp instructions per launch from
+    the committed ncu capture of the same workload, force kernel, cell size
+    and kernel sources; (None, reason) when no capture matches."""
+    try:
+        with open(COUNTERS) as f:
+            entries = json.load(f)["entries"]
+    except Exception:
+        return None, "no ncu capture committed"
+    dig = source_digest()
+    want = dict(workload=workload, force_variant_bits=variant & FORCE_BITS, cell_mult=cm)
+    for e in entries:
+        if all(e.get(k) == v for k, v in want.items()):
+            if e.get("source_digest") != dig:
+                return None, f"ncu capture is of other kernel sources ({e.get('source_digest')} vs {dig})"
+            return e, None
+    return None, f"no ncu capture of {want}"
+
+
+def ingest_ncu(raw_csv, workload, variant, cm, command, kernel="k_force"):
+    """Reads `ncu -i <report> --page raw --csv` output, takes the launches of
+    `kernel` (per launch: DRAM bytes read + written, warp instructions,
+    duration) and records their mean as the counters of this workload,
+    force kernel, cell size and kernel sources in profiles/."""
+    with open(raw_csv, newline="") as f:
+        rows = list(csv.reader(f))
+    head = rows[0]
+    units = rows[1]
+    col = {name: i for i, name in enumerate(head)}
+    scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9,
+             "nsecond": 1e-9, "usecond": 1e-6, "msecond": 1e-3, "second": 1.0, "inst": 1.0, "": 1.0}
+
+    def val(r, name):
+        i = col[name]
+        u = units[i].strip()
+        return float(r[i].replace(",", "")) * scale.get(u, 1.0)
+
+    launches = [r for r in rows[2:] if len(r) == len(head) and kernel in r[col["Kernel Name"]]]
+    if not launches:
+        raise SystemExit(f"no {kernel} launch in {raw_csv}")
+    rd = float(np.mean([val(r, "dram__bytes_read.sum") for r in launches]))
+    wr = float(np.mean([val(r, "dram__bytes_write.sum") for r in launches]))
+    inst = float(np.mean([val(r, "smsp__inst_executed.sum") for r in launches]))
+    dur = float(np.mean([val(r, "gpu__time_duration.sum") for r in launches]))
+    try:
+        commit = subprocess.run(["git", "-C", ROOT, "rev-parse", "--short", "HEAD"], capture_output=True,
+                                text=True).stdout.strip() or None
+    except Exception:
+        commit = None
+    entry = dict(kernel=kernel, workload=workload, force_variant_bits=variant & FORCE_BITS, cell_mult=cm,
+                 variant=variant, source_digest=source_digest(), git_commit=commit, launches=len(launches),
+                 dram_bytes_read=rd, dram_bytes_write=wr, dram_bytes=rd + wr, warp_instructions=inst,
+                 ncu_duration_s=dur, command=command)
+    try:
+        with open(COUNTERS) as f:
+            data = json.load(f)
+    except Exception:
+        data = {"about": "ncu counters of the force kernel per launch (mean over the captured launches), "
+                         "read by bench.py for roofline.traffic and issue_roofline", "entries": []}
+    data["entries"] = [e for e in data["entries"]
+                       if not (e["workload"] == workload and e["force_variant_bits"] == entry["force_variant_bits"]
+                               and e["cell_mult"] == cm)] + [entry]
+    with open(COUNTERS, "w") as f:
+        json.dump(data, f, indent=1)
+        f.write("\n")
+    print(json.dumps(entry))
 
 
 class Clocks:
@@ -148,31 +260,48 @@ def cpu_sample(spec, budget_s=12.0, nthreads=0):
 
 
 def run_reference(args, spec, config):
+    """The reference arm: the reference's algorithm on the host cores.  Each
+    step is a bounded sample of the workload (the three all-pairs passes and
+    the integration of m particles against all n), sized so that the whole
+    run, warm-up included, takes about 150 s; `ms_per_step` is that sample
+    step's measured time, and the time a step of the whole workload would
+    take is reported beside it as an extrapolation.  Rank 0 alone runs."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     import oracle as O
 
     O.build()
-    # each step is a bounded sample of the workload, sized so that the whole
-    # run (warm-up included) takes about 150 s of CPU time at most
     budget = min(args.ref_seconds, max(0.5, 150.0 / max(args.steps + args.warmup, 1)))
-    vals = []
+    sizes, times = [], []
     cores = m = 0
     for _ in range(args.warmup):
         cpu_sample(spec, budget_s=budget)
     for _ in range(args.steps):
-        v, cores, m, _t = cpu_sample(spec, budget_s=budget)
-        vals.append(v)
-    val = float(np.median(vals))
-    line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": spec["n"] / val * 1e3,
+        _v, cores, m, t = cpu_sample(spec, budget_s=budget)
+        sizes.append(m)
+        times.append(t)
+    val = float(np.sum(sizes) / np.sum(times)) if times else 0.0
+    sample = f"{m} of {spec['n']} particles x 3 all-pairs passes + integration per step"
+    line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "impl": "reference", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times)) * 1e3,
+            "ms_per_step_kind": "measured per sample step (" + sample + ")",
+            "ms_per_step_full_workload": spec["n"] / val * 1e3 if val else None,
+            "ms_per_step_full_workload_kind": "extrapolated: the whole workload at the sampled rate",
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded lattice + fBm terrain)", "config": config,
-            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{m} of {spec['n']} particles x 3 all-pairs passes + integration per step"},
+            "cpu_baseline": dict({"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                                  "sample": sample}, **calibration_keys()),
             "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def calibration_keys():
+    c = port_calibration()
+    if not c:
+        return {}
+    return {"port_vs_reference": c["port_speed_over_reference"],
+            "port_vs_reference_note": c["note"]}
 
 
 def traversal(scene, step_ms):
@@ -190,12 +319,27 @@ def traversal(scene, step_ms):
 SPINUP = {"plain_1m": 1000, "plain_small": 500, "skew": 2000, "batched": 500}
 
 
-def spinup_steps(args):
-    return SPINUP.get(args.workload, 0) if args.spinup is None else args.spinup
+def spinup_steps(args, workload=None):
+    """Untimed steps before the warm-up: --spinup for the workload the
+    command names, the workload's mid-run default otherwise."""
+    w = workload or args.workload
+    if args.spinup is not None and w == args.workload:
+        return args.spinup
+    return SPINUP.get(w, 0)
 
 
 def flush_l2(buf):
     buf.zero_()
+
+
+def init_dist(ws):
+    """Gloo process group for the barrier and the max over ranks (the data
+    path has no collective)."""
+    if ws > 1:
+        import torch.distributed as dist
+
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
 
 
 def run_ours(args, spec, config):
@@ -205,10 +349,7 @@ def run_ours(args, spec, config):
     import workloads as W
 
     ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
+    init_dist(ws)
     torch.cuda.set_device(local)
     n = spec["n"]
     sysm = S.System(particle_capacity=n, key_capacity=1 << 20, terrain_capacity=1 << 21, tile=args.tile,
@@ -284,6 +425,18 @@ def run_ours(args, spec, config):
     os.remove(snap)
     os.rmdir(snap_dir)
     d = sc.diag()
+    dev_bytes = int(sysm.memory())
+    trav = traversal(sc, tot / args.steps) if rank == 0 else None
+    grid_cells = int(np.prod(sc.grid_dims()[:3]))
+    sysm.close()
+    del flush
+    torch.cuda.empty_cache()
+    # the batched and served forms, in the same run
+    extras = {}
+    if args.extras and spec["name"] == "plain_1m":
+        base_cfg = {"h": W.H, "dt": W.PHYS["dt"], "erosion": True, "tile": args.tile, "cell_mult": args.cell_mult}
+        extras["batched"] = run_batched(args, base_cfg, embedded=True)
+        extras["serving"] = run_serving(args, base_cfg, embedded=True)
     if rank != 0:
         return
     # roofline of the dominant kernel (the force stage): algorithmic bytes =
@@ -296,11 +449,11 @@ def run_ours(args, spec, config):
     force_bytes = 80.0 * n + 4.0 * texels
     achieved = force_bytes / (force_ms * 1e-3) / 1e9
     step_ms = tot / args.steps
-    ncells = int(np.prod(sc.grid_dims()[:3]))
-    step_bytes = 88.0 * n + 16.0 * ncells + 20.0 * texels
+    step_bytes = 88.0 * n + 16.0 * grid_cells + 20.0 * texels
     cpu_v, cores, m, _ = cpu_sample(spec, budget_s=args.ref_seconds)
     variant = tuned["variant"] if tuned else args.variant if args.variant is not None else 88
     cm = tuned["cell_mult"] if tuned else args.cell_mult
+    cnt, why = ncu_counters(config["workload"], variant, cm)
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -308,12 +461,15 @@ def run_ours(args, spec, config):
         "config": config,
         "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,
-                     "traffic": NCU_FORCE_TRAFFIC.get((config["workload"], variant & FORCE_BITS, cm)),
+                     "traffic": cnt["dram_bytes"] if cnt else None,
+                     "traffic_source": (f"ncu capture {cnt['source_digest']} ({cnt['command']})" if cnt else why),
+                     "algorithmic_bytes": force_bytes,
                      "peak_kind": kind,
                      "step_bytes_frac": step_bytes / (step_ms * 1e-3) / 1e9 / hbm},
-        "issue_roofline": issue_roofline(config["workload"], variant, cm, force_ms, clk.summary()),
-        "cpu_baseline": {"value": cpu_v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{m} of {n} particles x 3 all-pairs passes + integration per step"},
+        "issue_roofline": issue_roofline(cnt, force_ms, clk.summary()),
+        "cpu_baseline": dict({"value": cpu_v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                              "sample": f"{m} of {n} particles x 3 all-pairs passes + integration per step"},
+                             **calibration_keys()),
         "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": int(C_PARAMS_BYTES),
                 "d2h_bytes_per_step": int(n * 12), "readback": "asynchronous into pinned memory, overlapped"},
         "e2e_sync": {"value": e2e_sync, "unit": "particle-steps/s", "h2d_bytes_per_step": int(C_PARAMS_BYTES),
@@ -321,13 +477,17 @@ def run_ours(args, spec, config):
         "gpu_launches": int(args.steps * (7 if t else 6)),
         "stages_ms": {name: float(v) for name, v in zip(S.STAGES, stages)},
         "clocks": clk.summary(),
-        "device_bytes": int(sysm.memory()),
+        "device_bytes": dev_bytes,
         "mass_units_total": int(d["total_units"]),
         "diag_fp64": {"kinetic": d["kinetic"], "potential": d["potential"], "momentum": d["momentum"],
                       "nan_particles": d["nan_particles"]},
         "tuned": tuned,
-        "traversal": traversal(sc, step_ms),
+        "traversal": trav,
     }
+    line.update(extras)
+    if extras:
+        line["config"] = dict(config, batched=extras["batched"]["config"]["scenes_desc"],
+                              serving=extras["serving"]["config"]["trace_desc"])
     print(json.dumps(line), flush=True)
 
 
@@ -335,28 +495,13 @@ def run_ours(args, spec, config):
 # and its step budget (4 B) that set_params copies to the device.
 C_PARAMS_BYTES = 248 + 4
 
-# The variant bits that select the force kernel (4 register budget, 8 lists,
-# 16 list walk loaded ahead, 128 packed records); the others change only the
-# density pass, whose lists are the same in every variant.
-FORCE_BITS = 4 | 8 | 16 | 128
 
-# DRAM bytes (read + write) of one k_force launch, from an ncu capture of the
-# same workload at the same point of the run (mid-run) with kernel variant 88
-# (force bits 24) and cell_mult 0.5 (the neighbour lists the force pass reads
-# are most of it).  Reported only for that force kernel and cell size.
-NCU_FORCE_TRAFFIC = {("plain_1m", 24, 0.5): 404.4e6}
-# Warp instructions of one k_force launch (smsp__inst_executed.sum) from the
-# same capture: with the live kernel time they place the kernel against the
-# instruction-issue roofline (4 warp instructions per cycle per SM).
-NCU_FORCE_WARP_INST = {("plain_1m", 24, 0.5): 397.26e6}
-
-
-def issue_roofline(workload, variant, cm, force_ms, clocks):
+def issue_roofline(cnt, force_ms, clocks):
     """The force kernel against the instruction-issue peak: warp
-    instructions per launch (ncu, same configuration and point of the run)
-    over the live CUDA-event time, against 4 per cycle per SM at the
-    sampled SM clock."""
-    inst = NCU_FORCE_WARP_INST.get((workload, variant & FORCE_BITS, cm))
+    instructions per launch (the ncu capture of the same workload, force
+    kernel, cell size and sources) over the live CUDA-event time, against 4
+    per cycle per SM at the sampled SM clock."""
+    inst = cnt["warp_instructions"] if cnt else None
     if inst is None or not force_ms:
         return None
     import torch
@@ -375,10 +520,7 @@ def _init_ranks():
     import torch
 
     ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
+    init_dist(ws)
     torch.cuda.set_device(local)
     return ws, rank, local
 
@@ -393,11 +535,12 @@ def _gather(value, ws):
     return out
 
 
-def run_batched(args, config):
+def run_batched(args, config, embedded=False):
     """Batched form vs plain form on the same seeded scenes: all scenes in one
     system (one launch per stage for all of them, 16-step CUDA graphs) against
     each scene alone in its own system, timed scene after scene.  With N ranks
-    each rank runs its cost-balanced share of the scenes."""
+    each rank runs its cost-balanced share of the scenes.  Returns the
+    result on rank 0 (embedded) or prints it as a line of its own."""
     import shard
     import sph_gb300 as S
     import workloads as W
@@ -413,7 +556,7 @@ def run_batched(args, config):
     scenes = [sysm.scene_from_request(base, r) for r in reqs]
     # spin-up (untimed), then each scene's state is checkpointed so that the
     # plain form starts every scene from the same state
-    spin = spinup_steps(args)
+    spin = spinup_steps(args, "batched")
     tmp = tempfile.mkdtemp(prefix="sph_bench_")
     if spin:
         sysm.step(spin)
@@ -431,17 +574,21 @@ def run_batched(args, config):
         for path in paths:
             os.remove(path)
         os.rmdir(tmp)
-        return
+        return None
+    d0 = sysm.diag_many(scenes)
     with Clocks() as clk:
         ms = barrier_max(sysm.time_steps(args.steps), ws)
+    d1 = sysm.diag_many(scenes)
     batched = total_all * args.steps / (ms * 1e-3)
+    bad = sum(1 for d in d1 if d["total_units"] != 0 or d["nan_particles"] != 0)
     sysm.close()
     # plain form: one system per scene, same steps, same tuned tile and cell
     tile = tuned["tile"] if tuned else args.tile
     cm = tuned["cell_mult"] if tuned else args.cell_mult
     variant = tuned["variant"] if tuned else args.variant
     plain_ms = 0.0
-    for r, path in zip(reqs, paths):
+    same = 0
+    for r, path, a in zip(reqs, paths, d1):
         with S.System(particle_capacity=r["particles"], tile=tile, graph_steps=16, device=local,
                       variant=variant) as one:
             sc1 = one.scene_from_request(W.base_params(cm), r)
@@ -450,29 +597,42 @@ def run_batched(args, config):
             one.step(args.warmup)
             one.sync()
             plain_ms += one.time_steps(args.steps)
+            # the scene alone ends where it ended in the batch, bit for bit
+            same += int(sc1.diag()["state_hash"] == a["state_hash"])
     os.rmdir(tmp)
     plain_ms = barrier_max(plain_ms, ws)
     plain = total_all * args.steps / (plain_ms * 1e-3)
+    same = sum(_gather(same, ws))
+    bad = sum(_gather(bad, ws))
     if rank != 0:
-        return
-    line = {"metric": METRIC, "value": batched, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-            "config": dict(config, workload="batched", scenes=len(all_reqs), particles=total_all,
-                           parallelism=f"scenes sharded over {ws} rank(s)",
-                           l2="inputs larger than L2 (%.0f MB of particle state)" % (total_all * 100 / 1e6)),
-            "plain_value": plain, "batched_over_plain": batched / plain, "plain_ms_per_step": plain_ms / args.steps,
-            "tuned": tuned, "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
+        return None
+    window = (f"steps {spin + args.warmup + 1}..{spin + args.warmup + args.steps} after {spin} untimed spin-up "
+              f"steps")
+    desc = (f"{len(all_reqs)} seeded scenes, {total_all} particles (2,048-131,072 each, log-uniform), "
+            f"terrain sides 64-512, {window}")
+    res = {"metric": METRIC, "value": batched, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
+           "config": dict(config, workload="batched", scenes=len(all_reqs), particles=total_all, window=window,
+                          parallelism=f"scenes sharded over {ws} rank(s)", scenes_desc=desc,
+                          l2="inputs larger than L2 (%.0f MB of particle state)" % (total_all * 100 / 1e6)),
+           "plain_value": plain, "batched_over_plain": batched / plain, "plain_ms_per_step": plain_ms / args.steps,
+           "alone_equals_batched": f"{same} of {len(all_reqs)} scenes (state fingerprint after the timed steps)",
+           "mass_violations": bad, "tuned": tuned, "clocks": clk.summary()}
+    if embedded:
+        return {k: res[k] for k in ("value", "unit", "ms_per_step", "plain_value", "plain_ms_per_step",
+                                    "batched_over_plain", "alone_equals_batched", "mass_violations", "tuned",
+                                    "clocks", "config")}
+    print(json.dumps(res), flush=True)
+    return None
 
 
-def run_serving(args, config):
+def run_serving(args, config, embedded=False):
     """Served form: a Poisson request trace replayed in real time through the
     continuous-batching server.  With N ranks each rank serves its
     cost-balanced share of the trace; throughput is the job's particle-steps
-    over the slowest rank's wall time, latencies are pooled."""
-    import numpy as np
-
+    over the slowest rank's wall time, latencies are pooled.  Returns the
+    result on rank 0 (embedded) or prints it as a line of its own."""
     import shard
     import sph_gb300 as S
     import workloads as W
@@ -490,7 +650,7 @@ def run_serving(args, config):
                          peak_p=st["peak_particles"], peak_b=st["peak_bytes"], chunks=st["chunks"],
                          phases={k: st[k] for k in ("admit_s", "prepare_s", "gpu_wait_s", "retire_s")}), ws)
     if rank != 0:
-        return
+        return None
     lat = np.sort(np.concatenate([np.asarray(q["lat"]) for q in parts]))
 
     def pct(q):
@@ -498,20 +658,54 @@ def run_serving(args, config):
 
     wall = max(q["wall"] for q in parts)
     ps = sum(q["ps"] for q in parts)
-    line = {"metric": METRIC, "value": ps / wall, "unit": "particle-steps/s", "n_gpus": ws,
-            "steps": int(sum(r["steps"] for r in full)), "warmup": 0, "ms_per_step": None,
-            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded Poisson request trace)",
-            "config": dict(config, workload="serving", requests=len(full), rate_per_s=args.rate,
-                           hbm_budget_gb=120, parallelism=f"requests sharded over {ws} rank(s)",
-                           policy=args.policy, max_active_particles=args.max_active),
-            "p50_latency_s": pct(0.50), "p99_latency_s": pct(0.99), "max_latency_s": float(lat[-1]),
-            "wall_s": wall, "peak_active": max(q["peak"] for q in parts),
-            "peak_particles": max(q["peak_p"] for q in parts), "peak_bytes": max(q["peak_b"] for q in parts),
-            "chunks": sum(q["chunks"] for q in parts), "mass_violations": sum(q["bad"] for q in parts),
-            "host_phases_s": parts[0]["phases"],
-            "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
+    desc = (f"{len(full)} seeded requests, Poisson at {args.rate:g}/s, 4,096-262,144 particles, "
+            f"100-2,000 steps, 120 GB budget, admission {args.policy}")
+    out = {"metric": METRIC, "value": ps / wall, "unit": "particle-steps/s", "n_gpus": ws,
+           "steps": int(sum(r["steps"] for r in full)), "warmup": 0, "ms_per_step": None,
+           "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded Poisson request trace)",
+           "config": dict(config, workload="serving", requests=len(full), rate_per_s=args.rate,
+                          hbm_budget_gb=120, parallelism=f"requests sharded over {ws} rank(s)",
+                          policy=args.policy, max_active_particles=args.max_active, trace_desc=desc),
+           "p50_latency_s": pct(0.50), "p99_latency_s": pct(0.99), "max_latency_s": float(lat[-1]),
+           "requests": int(len(lat)), "wall_s": wall, "peak_active": max(q["peak"] for q in parts),
+           "peak_particles": max(q["peak_p"] for q in parts), "peak_bytes": max(q["peak_b"] for q in parts),
+           "chunks": sum(q["chunks"] for q in parts), "mass_violations": sum(q["bad"] for q in parts),
+           "host_phases_s": parts[0]["phases"],
+           "clocks": clk.summary()}
+    if embedded:
+        return {k: out[k] for k in ("value", "unit", "p50_latency_s", "p99_latency_s", "max_latency_s", "requests",
+                                    "wall_s", "peak_active", "peak_particles", "mass_violations", "host_phases_s",
+                                    "clocks", "config")}
+    print(json.dumps(out), flush=True)
+    return None
+
+
+def free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_ranks(n):
+    """Re-executes this command as n ranks, one process per GPU, through
+    torch.distributed.run; returns its exit status."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.abspath(__file__),
+           *sys.argv[1:]]
+    return subprocess.run(cmd).returncode
+
+
+def dry_run(args):
+    """The rank plumbing without CUDA: every rank takes part in the barrier
+    and the max over ranks; rank 0 prints what the real line's rank fields
+    would hold."""
+    ws, rank, _ = dist_env()
+    init_dist(ws)
+    t = barrier_max(0.001 * (rank + 1), ws)
+    if rank == 0:
+        print(json.dumps({"dry_run": True, "impl": args.impl, "n_gpus": ws, "steps": args.steps,
+                          "warmup": args.warmup, "max_over_ranks_s": t, "workload": args.workload}), flush=True)
 
 
 def main():
@@ -545,14 +739,31 @@ def main():
                     help="plain workloads: start from a checkpoint instead of the spin-up (short profiler runs)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="warm-up and timed steps only (for profiler captures); prints nothing")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="plain_1m: leave out the batched and served forms measured in the same run")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="rank plumbing only, without CUDA: each rank joins the barrier, rank 0 prints n_gpus")
+    ap.add_argument("--ingest-ncu", default=None, metavar="RAW_CSV",
+                    help="record the force kernel's counters from `ncu -i REPORT --page raw --csv` output for "
+                         "--workload/--variant/--cell-mult into profiles/counters_k_force.json")
+    ap.add_argument("--ingest-command", default="", help="with --ingest-ncu: the capture command, as run")
     args = ap.parse_args()
+    if args.ingest_ncu:
+        ingest_ncu(args.ingest_ncu, args.workload, args.variant if args.variant is not None else 88, args.cell_mult,
+                   args.ingest_command)
+        return
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        sys.exit(launch_ranks(args.gpus))
+    ws = dist_env()[0]
+    if "WORLD_SIZE" in os.environ and ws != args.gpus:
+        print(f"bench: --gpus {args.gpus} but WORLD_SIZE={ws}; n_gpus reports the ranks running", file=sys.stderr)
+    if args.dry_run:
+        dry_run(args)
+        return
     import workloads as W
 
     if args.workload in ("batched", "serving") and args.impl == "ours":
         cfg = {"h": W.H, "dt": W.PHYS["dt"], "erosion": True, "tile": args.tile, "cell_mult": args.cell_mult}
-        if args.workload == "batched":
-            cfg["window"] = (f"steps {spinup_steps(args) + args.warmup + 1}..{spinup_steps(args) + args.warmup + args.steps}"
-                             f" after {spinup_steps(args)} untimed spin-up steps")
         (run_batched if args.workload == "batched" else run_serving)(args, cfg)
         return
     spec = {"plain_small": W.plain_small, "skew": lambda: W.skew_rain(args.particles)}.get(args.workload, W.plain_1m)()

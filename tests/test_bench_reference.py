@@ -24,5 +24,26 @@ def test_reference_arm_json_line():
     assert line["config"]["workload"] == "plain_small" and line["config"]["particles"] == 16384
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["value"] == line["value"] and cb["cores"] >= 1
+    assert cb["port_vs_reference"] > 0  # the port's speed against the reference's own Run
+    # ms_per_step is the measured sample step, which fits in the run; the
+    # whole-workload step is an extrapolation reported beside it
+    assert line["ms_per_step"] * (line["steps"] + line["warmup"]) / 1e3 < 600
+    assert line["ms_per_step_full_workload"] > line["ms_per_step"]
+    assert "extrapolated" in line["ms_per_step_full_workload_kind"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_gpus_flag_launches_ranks_dry_run():
+    """--gpus 2 without a launcher starts two ranks itself (gloo here, no
+    CUDA in the dry run); both join the barrier and rank 0 reports n_gpus 2,
+    for either arm."""
+    for impl in ("ours", "reference"):
+        cmd = [sys.executable, "bench.py", "--gpus", "2", "--dry-run", "--impl", impl, "--steps", "1", "--warmup", "0"]
+        env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+        r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300, env=env)
+        assert r.returncode == 0, r.stderr[-2000:]
+        lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+        assert len(lines) == 1, r.stdout
+        assert lines[0]["n_gpus"] == 2 and lines[0]["dry_run"] and lines[0]["impl"] == impl
+        assert lines[0]["max_over_ranks_s"] == 0.002  # rank 1's value: the max over ranks
