@@ -122,7 +122,12 @@ typedef struct sph_system_config {
                                 32 = with 8: relaxed register budget of the density pass only,
                                 64 = with 8: the density pass loads candidates in pairs,
                                128 = with 8: the force pass gathers one packed 32-byte
-                                     record per neighbour (32 more bytes per particle);
+                                     record per neighbour (32 more bytes per particle),
+                               256 = with 8: cooperative passes, a group of lanes per
+                                     particle: the density pass sweeps the particle's
+                                     candidates 32 at a time (2048: 16 lanes), the force
+                                     pass splits its list over 8 lanes (512: 4, 1024: 16);
+                                     with 256, bit 4 relaxes the force pass's registers;
                                 default 88 (8 + 16 + 64) */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;
@@ -172,10 +177,10 @@ typedef struct sph_tune_result {
     int variant;
     float ms_per_step;
     int n_tried;
-    int tiles[32];
-    float cell_mults[32];
-    int variants[32];
-    float ms[32];
+    int tiles[64];
+    float cell_mults[64];
+    int variants[64];
+    float ms[64];
 } sph_tune_result;
 SPH_API int sph_system_autotune(sph_system* s, int steps, sph_tune_result* out);
 
@@ -228,7 +233,10 @@ SPH_API int sph_scenes_diag(sph_system* s, int k, const int* scenes, sph_diag* o
 
 /* ---- terrain (Grid heightfield, grid.h:43-116) ---------------------------- */
 /* LoadHeightfield generalised to any size and FP32 metres above the box floor
- * (grid.h:98-102); resets the int64 erosion deltas to zero. */
+ * (grid.h:98-102); resets the int64 erosion deltas to zero.  w = d = 0
+ * (heights may be NULL) removes the scene's terrain: the step then has no
+ * terrain contact and no erosion, as the reference's step, which never reads
+ * its Grid. */
 SPH_API int sph_scene_set_terrain(sph_system* s, int scene, int w, int d, const float* heights);
 /* Seeded fBm value noise (kind 0), ridged fBm (kind 1) or carved valleys
  * (kind 2: amplitude minus the ridged field, sharp valleys cut into a
@@ -255,6 +263,14 @@ SPH_API int sph_terrain_mesh_u8(const unsigned char* map512, int dimx, int dimy,
  * units: tw * td vertices (x, y, z, normal), z-major, and
  * 6 (tw - 1)(td - 1) indices.  The front end's per-frame terrain redraw. */
 SPH_API int sph_scene_terrain_mesh(sph_system* s, int scene, float* verts, unsigned* indices);
+/* The same mesh in the units of the reference's Grid, for a front end that
+ * draws the eroded terrain where Grid::UpdateGrid (grid.h:138-176) drew the
+ * loaded one: vertex (x, H / metres_per_level, z) for vertex indices x < tw,
+ * z < td (heights in grey levels, fractional once eroded), the normal the
+ * normalised sum of the four cross products of its edge vectors in those
+ * units; indices as genIndices (grid.h:118-136). */
+SPH_API int sph_scene_terrain_mesh_levels(sph_system* s, int scene, float metres_per_level, float* verts,
+                                          unsigned* indices);
 
 /* Grid::collision (Erosion/grid.h:462-805) for n queries at once: the
  * contact of a particle moving from cur to next with velocity vel against
@@ -392,11 +408,13 @@ SPH_API int sph_server_run_trace(sph_server* s, const sph_request* reqs, int n, 
  * array of SPH_STATIC_SCRATCH_BYTES that every GPU loading the library holds
  * until the process exits.  Limits: n <= SPH_STATIC_MAX_PARTICLES and a
  * uniform grid of at most SPH_STATIC_MAX_KEYS keys; larger requests return
- * SPH_ERR_CAPACITY.  The first call on a device resolves the array's device
- * address with that device current; make that first call before any stream
- * capture.  All calls share the array: calls whose work overlaps on the GPU
- * (other streams or host threads) race and must be serialised by the
- * caller. */
+ * SPH_ERR_CAPACITY; parameters are checked as by sph_scene_create.  The
+ * first call on a device resolves the array's device address with that
+ * device current.  Every call synchronises its stream before returning, so
+ * it must not be called on a stream that is being captured into a CUDA
+ * graph: such a call returns SPH_ERR_INVALID without touching the stream.
+ * All calls share the array: calls whose work overlaps on the GPU (other
+ * streams or host threads) race and must be serialised by the caller. */
 #define SPH_STATIC_MAX_PARTICLES 32768
 #define SPH_STATIC_MAX_KEYS 262144
 #define SPH_STATIC_MAX_TABLE 4096

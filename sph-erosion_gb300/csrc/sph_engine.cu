@@ -535,7 +535,7 @@ void System::upload_scene(int id) {
     SPH_CK(cudaEventRecord(up_ev_[k], st_));
 }
 
-static void validate(const sph_params& p) {
+void validate_params(const sph_params& p) {
     if (!(p.smoothing_radius > 0.0f) || !std::isfinite(p.smoothing_radius))
         throw Error(SPH_ERR_INVALID, "smoothing_radius must be positive");
     for (int a = 0; a < 3; ++a)
@@ -545,7 +545,7 @@ static void validate(const sph_params& p) {
 }
 
 int System::create_scene(const sph_params& p, int capacity, int tw, int td) {
-    validate(p);
+    validate_params(p);
     if (capacity < 0 || tw < 0 || td < 0) throw Error(SPH_ERR_INVALID, "negative size");
     if ((tw > 0) != (td > 0) || (tw > 0 && (tw < 2 || td < 2)))
         throw Error(SPH_ERR_INVALID, "terrain needs at least 2 x 2 vertices");
@@ -630,7 +630,7 @@ void System::destroy_scene(int id) {
 }
 
 void System::set_params(int id, const sph_params& p) {
-    validate(p);
+    validate_params(p);
     Scene& sc = scene(id);
     Scene ng = sc;
     ng.prm = p;
@@ -933,8 +933,18 @@ void System::upload_terrain_height(Scene& sc) {
 }
 
 void System::set_terrain(int id, int w, int d, const float* heights) {
-    if (w < 2 || d < 2 || !heights) throw Error(SPH_ERR_INVALID, "terrain needs at least 2 x 2 heights");
     Scene& sc = scene(id);
+    if (w == 0 && d == 0) {
+        // no terrain: the step's contact and erosion are off for this scene
+        SPH_CK(cudaStreamSynchronize(st_));
+        if (sc.tw > 0) ta_.release(sc.t_off, round_up((int64_t)sc.tw * sc.td, kTAlign));
+        sc.tw = sc.td = 0;
+        sc.t_off = 0;
+        upload_scene(id);
+        work_dirty_ = true;
+        return;
+    }
+    if (w < 2 || d < 2 || !heights) throw Error(SPH_ERR_INVALID, "terrain needs at least 2 x 2 heights");
     SPH_CK(cudaStreamSynchronize(st_));
     if (w != sc.tw || d != sc.td) {
         if (sc.tw > 0) ta_.release(sc.t_off, round_up((int64_t)sc.tw * sc.td, kTAlign));
@@ -1375,7 +1385,12 @@ void System::autotune(int steps, sph_tune_result* out) {
     };
     const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
-    const int variants[] = {0, 4, 28, 88, 120, 216};
+    // per-lane passes (0, 4: cells; 28, 88, 120, 216: lists) and cooperative
+    // passes (264: 32 + 8 lanes per particle, 268 with relaxed force
+    // registers, 392 packed records, 776 and 1288: 4 and 16 force lanes,
+    // 2312: 16 density lanes)
+    const int variants[] = {0, 4, 28, 88, 120, 216, 264, 268, 392, 776, 1288, 2312};
+    static_assert(2 * 2 * (sizeof variants / sizeof variants[0]) <= 64, "sph_tune_result holds 64 trials");
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;
     float bc = scenes_.empty() ? 1.0f : scenes_[0].prm.cell_mult;

@@ -78,6 +78,10 @@ struct Scene {
     SceneDev dev{};
 };
 
+// The checks every entry point applies to a parameter block: finite
+// positive smoothing radius and box half extents, cell_mult in [0.25, 8].
+void validate_params(const sph_params& p);
+
 class System {
    public:
     explicit System(const sph_system_config& cfg);

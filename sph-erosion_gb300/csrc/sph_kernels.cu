@@ -742,6 +742,101 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
     }
 }
 
+// Pass-2 results (fluid_system.h:151-154), pass 3 (:163, :177) and advance
+// (:306-353) with the terrain contact, the box collision and the erosion
+// exchange, from a particle's neighbour sums; only a writer stores the state
+// and the record and adds the exchange to the terrain.
+__device__ __forceinline__ void integrate_and_store(const DevArrays& a, const SceneDev& S, int p, float4 xi, float4 vi,
+                                                    float rho, const ForceAcc& acc, bool writer) {
+    // pass-2 results (:151-154) and pass 3 (:163, :177)
+    const float Fpx = -fm(acc.fpx, rho), Fpy = -fm(acc.fpy, rho), Fpz = -fm(acc.fpz, rho);
+    const float Fvx = fm(acc.fvx, S.visc), Fvy = fm(acc.fvy, S.visc), Fvz = fm(acc.fvz, S.visc);
+    const float Fgx = fm(rho, S.g[0]), Fgy = fm(rho, S.g[1]), Fgz = fm(rho, S.g[2]);
+    const float nsig = fm(-S.sigma, acc.cfl);
+    const float Fsx = fm(nsig, acc.nx), Fsy = fm(nsig, acc.ny), Fsz = fm(nsig, acc.nz);
+    // advance (:318-331)
+    const float Fx = fa(fa(Fpx, Fvx), fa(Fgx, Fsx));
+    const float Fy = fa(fa(Fpy, Fvy), fa(Fgy, Fsy));
+    const float Fz = fa(fa(Fpz, Fvz), fa(Fgz, Fsz));
+    const float ax = fdv(Fx, rho), ay = fdv(Fy, rho), az = fdv(Fz, rho);
+    const float dt = S.dt;
+    float vx = fa(vi.x, fm(ax, dt)), vy = fa(vi.y, fm(ay, dt)), vz = fa(vi.z, fm(az, dt));
+    float px = fa(xi.x, fm(vx, dt)), py = fa(xi.y, fm(vy, dt)), pz = fa(xi.z, fm(vz, dt));
+
+    const bool has_t = (S.flags & kFlagTerrain) != 0;
+    TSample ts;
+    if (has_t) {
+        ts = terrain_at(S, a.theight, px, pz);
+        if (py < ts.y && dt != 0.0f) {
+            const float d = fs(ts.y, py);
+            const float vdn = fa(fa(fm(vx, ts.nx), fm(vy, ts.ny)), fm(vz, ts.nz));
+            if (vdn < 0.0f) {
+                const float sp = len3(vx, vy, vz);
+                const float f = fa(1.0f, sp > 0.0f ? fdv(fm(S.cr, d), fm(dt, sp)) : 0.0f);
+                vx = fs(vx, fm(fm(ts.nx, f), vdn));
+                vy = fs(vy, fm(fm(ts.ny, f), vdn));
+                vz = fs(vz, fm(fm(ts.nz, f), vdn));
+            }
+            py = ts.y;
+        }
+    }
+    bool moved = false;
+    {
+        float cp[3], nr[3];
+        if (box_collide(S, px, py, pz, cp, nr) && dt != 0.0f) {
+            const float d = len3(fs(px, cp[0]), fs(py, cp[1]), fs(pz, cp[2]));
+            const float f = fa(1.0f, fdv(fm(0.5f, d), fm(dt, len3(vx, vy, vz))));
+            const float vdn = fa(fa(fm(vx, nr[0]), fm(vy, nr[1])), fm(vz, nr[2]));
+            vx = fs(vx, fm(fm(nr[0], f), vdn));
+            vy = fs(vy, fm(fm(nr[1], f), vdn));
+            vz = fs(vz, fm(fm(nr[2], f), vdn));
+            moved = px != cp[0] || pz != cp[2];
+            px = cp[0];
+            py = cp[1];
+            pz = cp[2];
+        }
+    }
+    int sed = __float_as_int(vi.w);
+    if (has_t && (S.flags & kFlagErosion)) {
+        // the exchange uses the surface under the particle's final
+        // position: a wall that moved it in x or z moved it to another
+        // sample of the terrain
+        if (moved) ts = terrain_at(S, a.theight, px, pz);
+        const float e = fs(py, ts.y);
+        if (e <= S.layer) {
+            float capf = fm(S.k_capacity, len3(vx, vy, vz));
+            if (capf > 1.0f) capf = 1.0f;
+            const float cap = fm(capf, 1073741824.0f);
+            const float s = __int2float_rn(sed);
+            const float q = (s < cap) ? fm(fm(S.k_pick, dt), fs(cap, s)) : -fm(fm(S.k_dep, dt), fs(s, cap));
+            if (q == q) {
+                long long Q = __float2ll_rn(q);
+                if ((long long)sed + Q < 0) Q = -(long long)sed;
+                if ((long long)sed + Q > 1073741824LL) Q = 1073741824LL - (long long)sed;
+                if (Q != 0) {
+                    sed += (int)Q;
+                    if (writer)
+                        atomicAdd(reinterpret_cast<unsigned long long*>(a.tdelta + S.t_off + ts.vnear),
+                                  (unsigned long long)(-Q));
+                }
+            }
+        }
+    }
+    if (!writer) return;
+    a.pos[p] = make_float4(px, py, pz, xi.w);
+    a.vel[p] = make_float4(vx, vy, vz, __int_as_float(sed));
+    if (S.flags & kFlagRecord) {
+        float* r = a.rec + (size_t)p * kRecFloats;
+        r[0] = ax; r[1] = ay; r[2] = az;
+        r[3] = Fpx; r[4] = Fpy; r[5] = Fpz;
+        r[6] = Fvx; r[7] = Fvy; r[8] = Fvz;
+        r[9] = Fgx; r[10] = Fgy; r[11] = Fgz;
+        r[12] = Fsx; r[13] = Fsy; r[14] = Fsz;
+        r[15] = acc.nx; r[16] = acc.ny; r[17] = acc.nz;
+        a.nbid[p] = acc.any ? acc.nb : a.snbid[p];
+    }
+}
+
 // force: passes 2 and 3 (fluid_system.h:127-178) and advance (:306-353) with
 // the terrain contact, the box collision and the erosion exchange.
 // NL: the in-range neighbours come from the lists the density pass wrote
@@ -857,90 +952,267 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
             }
             if (!valid) continue;
         }
-        // pass-2 results (:151-154) and pass 3 (:163, :177)
-        const float Fpx = -fm(acc.fpx, rho), Fpy = -fm(acc.fpy, rho), Fpz = -fm(acc.fpz, rho);
-        const float Fvx = fm(acc.fvx, S.visc), Fvy = fm(acc.fvy, S.visc), Fvz = fm(acc.fvz, S.visc);
-        const float Fgx = fm(rho, S.g[0]), Fgy = fm(rho, S.g[1]), Fgz = fm(rho, S.g[2]);
-        const float nsig = fm(-S.sigma, acc.cfl);
-        const float Fsx = fm(nsig, acc.nx), Fsy = fm(nsig, acc.ny), Fsz = fm(nsig, acc.nz);
-        // advance (:318-331)
-        const float Fx = fa(fa(Fpx, Fvx), fa(Fgx, Fsx));
-        const float Fy = fa(fa(Fpy, Fvy), fa(Fgy, Fsy));
-        const float Fz = fa(fa(Fpz, Fvz), fa(Fgz, Fsz));
-        const float ax = fdv(Fx, rho), ay = fdv(Fy, rho), az = fdv(Fz, rho);
-        const float dt = S.dt;
-        float vx = fa(vi.x, fm(ax, dt)), vy = fa(vi.y, fm(ay, dt)), vz = fa(vi.z, fm(az, dt));
-        float px = fa(xi.x, fm(vx, dt)), py = fa(xi.y, fm(vy, dt)), pz = fa(xi.z, fm(vz, dt));
+        integrate_and_store(a, S, p, xi, vi, rho, acc, true);
+    }
+}
 
-        const bool has_t = (S.flags & kFlagTerrain) != 0;
-        TSample ts;
-        if (has_t) {
-            ts = terrain_at(S, a.theight, px, pz);
-            if (py < ts.y && dt != 0.0f) {
-                const float d = fs(ts.y, py);
-                const float vdn = fa(fa(fm(vx, ts.nx), fm(vy, ts.ny)), fm(vz, ts.nz));
-                if (vdn < 0.0f) {
-                    const float sp = len3(vx, vy, vz);
-                    const float f = fa(1.0f, sp > 0.0f ? fdv(fm(S.cr, d), fm(dt, sp)) : 0.0f);
-                    vx = fs(vx, fm(fm(ts.nx, f), vdn));
-                    vy = fs(vy, fm(fm(ts.ny, f), vdn));
-                    vz = fs(vz, fm(fm(ts.nz, f), vdn));
-                }
-                py = ts.y;
-            }
+// ---------------------------------------------------------------------------
+// Cooperative neighbour passes (variant bit 8): a group of G lanes shares one
+// particle.  The lists the density pass hands to the force pass are
+// particle-major here (particle p's entries at p * kNbCap + q), which both
+// passes read and write in contiguous runs.
+
+// Range [st, en) of stencil row r of the particle at probe q: rows in the
+// order of for_rows (dz outer, dy inner, both ascending), trimmed the same
+// way, so a particle's candidates come in the same order.  gx2 holds the
+// squared x-gaps of cells cx - R .. cx + R (R = 1, 2; unused for R = 0, the
+// general reach).
+template <int R>
+__device__ __forceinline__ void stencil_row(const DevArrays& a, const SceneDev& S, const Probe& q, const float* gx2,
+                                            int r, uint32_t& st, uint32_t& en) {
+    st = en = 0;
+    const int side = R > 0 ? 2 * R + 1 : 2 * S.reach + 1;
+    const int reach = R > 0 ? R : S.reach;
+    const int dz = r / side - reach, dy = r % side - reach;
+    const int z = q.c.cz + dz, y = q.c.cy + dy;
+    if (!q.finite || z < 0 || z >= S.nz || y < 0 || y >= S.ny) return;
+    const uint32_t* off = a.offsets + S.k_off;
+    if (R > 0) {
+        const float gz = cell_gap(q.tz, z, S.nz), gy = cell_gap(q.ty, y, S.ny);
+        const float r2 = S.hcell * S.hcell - gy * gy - gz * gz;
+        if (!(r2 >= 0.0f)) return;
+        int lo = 0, hi = 0;
+#pragma unroll
+        for (int d = 1; d <= (R > 0 ? R : 1); ++d) {
+            if (gx2[R - d] <= r2) lo = -d;
+            if (gx2[R + d] <= r2) hi = d;
         }
-        bool moved = false;
-        {
-            float cp[3], nr[3];
-            if (box_collide(S, px, py, pz, cp, nr) && dt != 0.0f) {
-                const float d = len3(fs(px, cp[0]), fs(py, cp[1]), fs(pz, cp[2]));
-                const float f = fa(1.0f, fdv(fm(0.5f, d), fm(dt, len3(vx, vy, vz))));
-                const float vdn = fa(fa(fm(vx, nr[0]), fm(vy, nr[1])), fm(vz, nr[2]));
-                vx = fs(vx, fm(fm(nr[0], f), vdn));
-                vy = fs(vy, fm(fm(nr[1], f), vdn));
-                vz = fs(vz, fm(fm(nr[2], f), vdn));
-                moved = px != cp[0] || pz != cp[2];
-                px = cp[0];
-                py = cp[1];
-                pz = cp[2];
+        const uint32_t row = row_key(a.tab, S, y, z);
+        st = __ldg(off + row + q.c.cx + lo);
+        en = __ldg(off + row + q.c.cx + hi + 1);
+    } else {
+        int xl, xh;
+        if (!row_span(S, q, y, z, &xl, &xh)) return;
+        const uint32_t row = row_key(a.tab, S, y, z);
+        st = __ldg(off + row + xl);
+        en = __ldg(off + row + xh + 1);
+    }
+}
+
+// Group geometry of G lanes per particle (G a power of two, 4..32).
+template <int G>
+struct Group {
+    int gl;         // lane within the group
+    int gbase;      // first lane of the group within the warp
+    unsigned mask;  // the group's lanes
+    __device__ __forceinline__ Group() {
+        const int lane = threadIdx.x & 31;
+        gl = lane & (G - 1);
+        gbase = lane & ~(G - 1);
+        mask = G == 32 ? kFull : (((1u << G) - 1u) << gbase);
+    }
+};
+
+// Sum over the group, the same bits in every lane (each butterfly step adds
+// two equal-rounded operands in either order), in a fixed order.
+template <int G>
+__device__ __forceinline__ float group_sum(float v, unsigned mask) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v = fa(v, __shfl_xor_sync(mask, v, o, G));
+    return v;
+}
+
+// density, cooperative: the group walks the particle's candidates as one
+// stream (row after row, ascending index within a row) in windows of G, one
+// candidate per lane, so neighbouring lanes load neighbouring particles.
+// Each lane sums its candidates' terms in stream order; the group's partial
+// sums are combined by group_sum.  In-range candidates are appended to the
+// particle's list in stream order (ballot + prefix count).
+template <int G, int R, bool PACK>
+__device__ __forceinline__ void density_coop_particle(const DevArrays& a, const SceneDev& S, int p, int* soff,
+                                                      const Group<G>& g) {
+    const float4 xi = a.spos[p];
+    const Probe q = probe_of(S, xi);
+    float gx2[2 * (R > 0 ? R : 1) + 1];
+    if (R > 0) {
+#pragma unroll
+        for (int d = -R; d <= R; ++d) {
+            const int k = q.c.cx + d;
+            float g2 = INFINITY;
+            if (k >= 0 && k < S.nx) {
+                const float gg = cell_gap(q.tx, k, S.nx);
+                g2 = gg * gg;
             }
+            gx2[d + R] = g2;
         }
-        int sed = __float_as_int(vi.w);
-        if (has_t && (S.flags & kFlagErosion)) {
-            // the exchange uses the surface under the particle's final
-            // position: a wall that moved it in x or z moved it to another
-            // sample of the terrain
-            if (moved) ts = terrain_at(S, a.theight, px, pz);
-            const float e = fs(py, ts.y);
-            if (e <= S.layer) {
-                float capf = fm(S.k_capacity, len3(vx, vy, vz));
-                if (capf > 1.0f) capf = 1.0f;
-                const float cap = fm(capf, 1073741824.0f);
-                const float s = __int2float_rn(sed);
-                const float q = (s < cap) ? fm(fm(S.k_pick, dt), fs(cap, s)) : -fm(fm(S.k_dep, dt), fs(s, cap));
-                if (q == q) {
-                    long long Q = __float2ll_rn(q);
-                    if ((long long)sed + Q < 0) Q = -(long long)sed;
-                    if ((long long)sed + Q > 1073741824LL) Q = 1073741824LL - (long long)sed;
-                    if (Q != 0) {
-                        sed += (int)Q;
-                        atomicAdd(reinterpret_cast<unsigned long long*>(a.tdelta + S.t_off + ts.vnear),
-                                  (unsigned long long)(-Q));
+    }
+    const float4* sp = a.spos + S.p_off;
+    uint32_t* nl = a.nlist + (size_t)p * kNbCap;
+    const int side = R > 0 ? 2 * R + 1 : 2 * S.reach + 1;
+    const int nrows = side * side;
+    float rho = 0.0f;
+    int cnt = 0;
+    const unsigned below = (1u << g.gl) - 1u;
+    for (int rb = 0; rb < nrows; rb += G) {
+        uint32_t st = 0, en = 0;
+        if (rb + g.gl < nrows) stencil_row<R>(a, S, q, gx2, rb + g.gl, st, en);
+        const int len = (int)(en - st);
+        int inc = len;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            const int v = __shfl_up_sync(g.mask, inc, o, G);
+            if (g.gl >= o) inc += v;
+        }
+        const int pre = inc - len;
+        const int total = __shfl_sync(g.mask, inc, G - 1, G);
+        int carry = 0;
+        for (int wb = 0; wb < total; wb += G) {
+            // the rows that start in this window record where their
+            // candidates sit: candidate t of the stream is particle t + off
+            const bool starts = len > 0 && pre >= wb && pre < wb + G;
+            if (starts) soff[pre - wb] = (int)st - pre;
+            const unsigned m = __reduce_or_sync(g.mask, starts ? (1u << (pre - wb)) : 0u);
+            __syncwarp(g.mask);
+            const unsigned upto = m & ((2u << g.gl) - 1u);
+            const int off = upto ? soff[31 - __clz(upto)] : carry;
+            carry = m ? soff[31 - __clz(m)] : carry;
+            __syncwarp(g.mask);
+            const int t = wb + g.gl;
+            bool in = false;
+            uint32_t j = 0;
+            float s = 0.0f;
+            if (t < total) {
+                j = (uint32_t)(t + off);
+                const float4 xj = __ldg(sp + j);
+                s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
+                in = s <= S.smax;
+            }
+            if (in) rho = fa(rho, density_term(S, fsq(s)));
+            const unsigned b = (__ballot_sync(g.mask, in) & g.mask) >> g.gbase;
+            const int at = cnt + __popc(b & below);
+            if (in && at < kNbCap) nl[at] = j;
+            cnt += __popc(b);
+        }
+    }
+    rho = group_sum<G>(rho, g.mask);
+    if (g.gl == 0) {
+        const float P = fm(S.k, fs(rho, S.p0));
+        const float Ai = fdv(P, fm(rho, rho)), Bi = fdv(S.mass, rho);
+        a.dyn[p] = make_float4(rho, Ai, Bi, P);
+        a.ncnt[p] = cnt;
+        if (PACK) {
+            const float4 vi = a.svel[p];
+            a.fdat[2 * (size_t)p] = make_float4(xi.x, xi.y, xi.z, Ai);
+            a.fdat[2 * (size_t)p + 1] = make_float4(vi.x, vi.y, vi.z, Bi);
+        }
+    }
+}
+
+template <int G, bool PACK>
+__global__ void __launch_bounds__(256) k_density_coop(DevArrays a) {
+    __shared__ int s_off[256];
+    const Group<G> g;
+    int* soff = s_off + (threadIdx.x & ~(G - 1));
+    const int group = threadIdx.x / G, ngroups = blockDim.x / G;
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        if (S.flags & kFlagOrdered) continue;
+        const int end = min(wk.start + (int)blockDim.x, S.p_off + S.n);
+        for (int p = wk.start + group; p < end; p += ngroups) {
+            if (S.reach == 2)
+                density_coop_particle<G, 2, PACK>(a, S, p, soff, g);
+            else if (S.reach == 1)
+                density_coop_particle<G, 1, PACK>(a, S, p, soff, g);
+            else
+                density_coop_particle<G, 0, PACK>(a, S, p, soff, g);
+        }
+    }
+}
+
+// force, cooperative: the group splits the particle's list (lane gl takes
+// entries gl, gl + G, ...), each lane sums its pairs' terms in list order,
+// the group combines them with group_sum, and every lane of the group then
+// holds the particle's sums; the integration, contacts and erosion are
+// computed alike in every lane and written by lane 0.  A particle whose list
+// overflowed has the group split its cell rows instead (row r to lane r mod G).
+template <int G, bool PACK, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_force_coop(DevArrays a) {
+    const Group<G> g;
+    const int group = threadIdx.x / G, ngroups = blockDim.x / G;
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        if (S.flags & kFlagOrdered) continue;
+        const int end = min(wk.start + (int)blockDim.x, S.p_off + S.n);
+        for (int p = wk.start + group; p < end; p += ngroups) {
+            const int pl = p - S.p_off;
+            const float4 xi = a.spos[p];
+            const float4 vi = a.svel[p];
+            const float4 di = a.dyn[p];
+            const float rho = di.x, Ai = di.y;
+            ForceAcc acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, -1, 0};
+            const float4* sp = a.spos + S.p_off;
+            const float4* sv = a.svel + S.p_off;
+            const float4* sd = a.dyn + S.p_off;
+            const bool rec = (S.flags & kFlagRecord) != 0;
+            auto pair = [&](uint32_t j, float4 xj, float4 vj, float Aj, float Bj, int idj) {
+                const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
+                force_pair(S, acc, rx, ry, rz, fsq(dist2(rx, ry, rz)), vi.x, vi.y, vi.z, Ai, vj, Aj, Bj, idj,
+                           (int)j == pl);
+            };
+            const int cnt = a.ncnt[p];
+            if (cnt <= kNbCap) {
+                const uint32_t* nl = a.nlist + (size_t)p * kNbCap;
+                int qn = g.gl;
+                uint32_t j0 = qn < cnt ? __ldg(nl + qn) : 0u;
+                for (int qq = g.gl; qq < cnt; qq += G) {
+                    qn += G;
+                    const uint32_t j1 = qn < cnt ? __ldg(nl + qn) : 0u;  // next entry, loaded ahead
+                    if (PACK) {
+                        const float4* fd = a.fdat + 2 * (size_t)S.p_off;
+                        const float4 r0 = __ldg(fd + 2 * j0), r1 = __ldg(fd + 2 * j0 + 1);
+                        const int idj = rec ? __float_as_int(__ldg(&sp[j0].w)) : 0;
+                        pair(j0, r0, r1, r0.w, r1.w, idj);
+                    } else {
+                        const float4 xj = __ldg(sp + j0), vj = __ldg(sv + j0), dj = __ldg(sd + j0);
+                        pair(j0, xj, vj, dj.y, dj.z, __float_as_int(xj.w));
                     }
+                    j0 = j1;
                 }
+            } else {
+                int r = 0;
+                for_rows(a, S, xi, true, [&](uint32_t st, uint32_t en) {
+                    if ((r++ & (G - 1)) != g.gl) return;
+                    for (uint32_t j = st; j < en; ++j) {
+                        const float4 xj = __ldg(sp + j);
+                        if (dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z)) <= S.smax) {
+                            const float4 vj = __ldg(sv + j), dj = __ldg(sd + j);
+                            pair(j, xj, vj, dj.y, dj.z, __float_as_int(xj.w));
+                        }
+                    }
+                });
             }
-        }
-        a.pos[p] = make_float4(px, py, pz, xi.w);
-        a.vel[p] = make_float4(vx, vy, vz, __int_as_float(sed));
-        if (S.flags & kFlagRecord) {
-            float* r = a.rec + (size_t)p * kRecFloats;
-            r[0] = ax; r[1] = ay; r[2] = az;
-            r[3] = Fpx; r[4] = Fpy; r[5] = Fpz;
-            r[6] = Fvx; r[7] = Fvy; r[8] = Fvz;
-            r[9] = Fgx; r[10] = Fgy; r[11] = Fgz;
-            r[12] = Fsx; r[13] = Fsy; r[14] = Fsz;
-            r[15] = acc.nx; r[16] = acc.ny; r[17] = acc.nz;
-            a.nbid[p] = acc.any ? acc.nb : a.snbid[p];
+            acc.fpx = group_sum<G>(acc.fpx, g.mask);
+            acc.fpy = group_sum<G>(acc.fpy, g.mask);
+            acc.fpz = group_sum<G>(acc.fpz, g.mask);
+            acc.fvx = group_sum<G>(acc.fvx, g.mask);
+            acc.fvy = group_sum<G>(acc.fvy, g.mask);
+            acc.fvz = group_sum<G>(acc.fvz, g.mask);
+            acc.nx = group_sum<G>(acc.nx, g.mask);
+            acc.ny = group_sum<G>(acc.ny, g.mask);
+            acc.nz = group_sum<G>(acc.nz, g.mask);
+            acc.cfl = group_sum<G>(acc.cfl, g.mask);
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) {
+                acc.nb = max(acc.nb, __shfl_xor_sync(g.mask, acc.nb, o, G));
+                acc.any |= __shfl_xor_sync(g.mask, acc.any, o, G);
+            }
+            integrate_and_store(a, S, p, xi, vi, rho, acc, g.gl == 0);
         }
     }
 }
@@ -1175,7 +1447,63 @@ static void launch_density_nl(const DevArrays& a, const LaunchShape& s, cudaStre
         k_density<false, false, MINB, true, false, false><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 
+// Variant bit 8 (with bit 3): the cooperative passes, G lanes per particle.
+// Density: 32 lanes (bit 11: 16).  Force: 8 lanes (bit 9: 4, bit 10: 16).
+// Bit 7 packs the force-pass inputs as in the per-lane passes; bit 2
+// relaxes the force pass's register budget.
+static void launch_density_coop(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    const bool pack = (s.variant & 128) != 0;
+    if (s.variant & 2048) {
+        if (pack)
+            k_density_coop<16, true><<<s.grid_p, s.tile, 0, st>>>(a);
+        else
+            k_density_coop<16, false><<<s.grid_p, s.tile, 0, st>>>(a);
+    } else {
+        if (pack)
+            k_density_coop<32, true><<<s.grid_p, s.tile, 0, st>>>(a);
+        else
+            k_density_coop<32, false><<<s.grid_p, s.tile, 0, st>>>(a);
+    }
+}
+
+template <int MINB>
+static void launch_force_coop_b(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    const bool pack = (s.variant & 128) != 0;
+    const int gsel = (s.variant >> 9) & 3;
+    if (gsel == 1) {
+        if (pack)
+            k_force_coop<4, true, MINB><<<s.grid_p, s.tile, 0, st>>>(a);
+        else
+            k_force_coop<4, false, MINB><<<s.grid_p, s.tile, 0, st>>>(a);
+    } else if (gsel == 2) {
+        if (pack)
+            k_force_coop<16, true, MINB><<<s.grid_p, s.tile, 0, st>>>(a);
+        else
+            k_force_coop<16, false, MINB><<<s.grid_p, s.tile, 0, st>>>(a);
+    } else {
+        if (pack)
+            k_force_coop<8, true, MINB><<<s.grid_p, s.tile, 0, st>>>(a);
+        else
+            k_force_coop<8, false, MINB><<<s.grid_p, s.tile, 0, st>>>(a);
+    }
+}
+
+// Bit 2 relaxes the cooperative force pass's register budget (3 resident
+// blocks of 256 threads instead of 4).
+static void launch_force_coop(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    if (s.variant & 4)
+        launch_force_coop_b<3>(a, s, st);
+    else
+        launch_force_coop_b<4>(a, s, st);
+}
+
+static bool coop(const LaunchShape& s) { return (s.variant & (256 | 8)) == (256 | 8); }
+
 void launch_density(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    if (coop(s)) {
+        launch_density_coop(a, s, st);
+        return;
+    }
     const bool relaxed = (s.variant & 4) != 0;
     if (s.variant & 8) {
         if (relaxed)
@@ -1200,6 +1528,10 @@ void launch_density_ordered(const DevArrays& a, const LaunchShape& s, cudaStream
     k_density<true, false, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    if (coop(s)) {
+        launch_force_coop(a, s, st);
+        return;
+    }
     // the list variants walk their lists (or, on overflow, the cells) per
     // lane and need no shared memory
     if ((s.variant & 136) == 136) {

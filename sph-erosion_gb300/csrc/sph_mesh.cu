@@ -14,6 +14,7 @@
 // FP32 heights in world units, for the front end to redraw every frame.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <vector>
 
 #include "../../include/sph_erosion.h"
@@ -83,19 +84,23 @@ __global__ void k_mesh_indices(int dimx, int dimz, unsigned* __restrict__ idx) {
     o[5] = (unsigned)((j - 1) * dimx + i);
 }
 
-// World-space mesh of a scene's heights: vertex (x, floor + H, z) and the
-// normalised sum of the four cross products of its world-space edge vectors.
+// Mesh of a scene's heights: vertex (xlo + x sx, ylo + H ys, zlo + z sz) and
+// the normalised sum of the four cross products of its edge vectors in the
+// same units.  World units: ys = 1; the reference Grid's units (one unit per
+// vertex along x and z, heights in grey levels): sx = sz = 1, ys = 1 / metres
+// per level, origin 0.
 __global__ void k_mesh_f32(const float* __restrict__ h, int tw, int td, float xlo, float ylo, float zlo, float sx,
-                           float sz, float* __restrict__ out) {
+                           float sz, float ys, float* __restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= tw * td) return;
     const int z = t / tw, x = t - z * tw;
-    const float y = h[t];
+    auto H = [&](int q) { return fm(h[q], ys); };
+    const float y = H(t);
     V3 u{0.f, 0.f, 0.f}, d{0.f, 0.f, 0.f}, r{0.f, 0.f, 0.f}, l{0.f, 0.f, 0.f};
-    if (x > 0) l = V3{sx, fs(y, h[t - 1]), 0.0f};
-    if (x + 1 < tw) r = V3{sx, fs(h[t + 1], y), 0.0f};
-    if (z > 0) u = V3{0.0f, fs(y, h[t - tw]), sz};
-    if (z + 1 < td) d = V3{0.0f, fs(h[t + tw], y), sz};
+    if (x > 0) l = V3{sx, fs(y, H(t - 1)), 0.0f};
+    if (x + 1 < tw) r = V3{sx, fs(H(t + 1), y), 0.0f};
+    if (z > 0) u = V3{0.0f, fs(y, H(t - tw)), sz};
+    if (z + 1 < td) d = V3{0.0f, fs(H(t + tw), y), sz};
     const V3 n = normalize3(add3(add3(add3(cross3(u, l), cross3(u, r)), cross3(d, l)), cross3(d, r)));
     float* o = out + (size_t)6 * t;
     o[0] = fa(xlo, fm((float)x, sx));
@@ -137,21 +142,27 @@ void mesh_u8(const unsigned char* map_host, int dimx, int dimy, int dimz, float*
     if (idx && ni > 0) check_cuda(cudaMemcpy(idx, di.p, (size_t)ni * 4, cudaMemcpyDeviceToHost), "copy indices");
 }
 
-void mesh_scene(System& sys, int scene, float* verts, unsigned* idx) {
+// metres_per_level = 0: world units; > 0: the reference Grid's units.
+void mesh_scene(System& sys, int scene, float* verts, unsigned* idx, float metres_per_level) {
     int tw, td;
     sys.terrain_dims(scene, &tw, &td);
     if (tw < 2) throw Error(SPH_ERR_STATE, "scene has no terrain");
+    if (!(metres_per_level >= 0.0f) || !std::isfinite(metres_per_level))
+        throw Error(SPH_ERR_INVALID, "metres_per_level must be finite and >= 0");
     const sph_params& p = sys.params(scene);
-    const float sx = (p.box_half[0] + p.box_half[0]) / (float)(tw - 1);
-    const float sz = (p.box_half[2] + p.box_half[2]) / (float)(td - 1);
+    const bool grid_units = metres_per_level > 0.0f;
+    const float sx = grid_units ? 1.0f : (p.box_half[0] + p.box_half[0]) / (float)(tw - 1);
+    const float sz = grid_units ? 1.0f : (p.box_half[2] + p.box_half[2]) / (float)(td - 1);
+    const float ys = grid_units ? 1.0f / metres_per_level : 1.0f;
+    const float xlo = grid_units ? 0.0f : p.box_center[0] - p.box_half[0];
+    const float ylo = grid_units ? 0.0f : p.box_center[1] - p.box_half[1];
+    const float zlo = grid_units ? 0.0f : p.box_center[2] - p.box_half[2];
     const int64_t nv = (int64_t)tw * td, ni = (int64_t)6 * (tw - 1) * (td - 1);
     std::vector<float> h((size_t)nv);
     sys.get_terrain(scene, h.data(), nullptr);
     Tmp dh((size_t)nv * 4), dv((size_t)nv * 24), di((size_t)ni * 4);
     check_cuda(cudaMemcpy(dh.p, h.data(), (size_t)nv * 4, cudaMemcpyHostToDevice), "copy heights");
-    k_mesh_f32<<<(unsigned)((nv + 255) / 256), 256>>>(static_cast<float*>(dh.p), tw, td,
-                                                      p.box_center[0] - p.box_half[0], p.box_center[1] - p.box_half[1],
-                                                      p.box_center[2] - p.box_half[2], sx, sz,
+    k_mesh_f32<<<(unsigned)((nv + 255) / 256), 256>>>(static_cast<float*>(dh.p), tw, td, xlo, ylo, zlo, sx, sz, ys,
                                                       static_cast<float*>(dv.p));
     k_mesh_indices<<<(unsigned)((ni / 6 + 255) / 256), 256>>>(tw, td, static_cast<unsigned*>(di.p));
     check_cuda(cudaGetLastError(), "mesh kernels");
@@ -187,7 +198,16 @@ SPH_API int sph_terrain_mesh_u8(const unsigned char* map512, int dimx, int dimy,
 SPH_API int sph_scene_terrain_mesh(sph_system* s, int scene, float* verts, unsigned* indices) {
     return mesh_guard([&] {
         if (!s || !s->sys) throw sph::Error(SPH_ERR_INVALID, "null system handle");
-        sph::mesh_scene(*s->sys, scene, verts, indices);
+        sph::mesh_scene(*s->sys, scene, verts, indices, 0.0f);
+    });
+}
+
+SPH_API int sph_scene_terrain_mesh_levels(sph_system* s, int scene, float metres_per_level, float* verts,
+                                          unsigned* indices) {
+    return mesh_guard([&] {
+        if (!s || !s->sys) throw sph::Error(SPH_ERR_INVALID, "null system handle");
+        if (!(metres_per_level > 0.0f)) throw sph::Error(SPH_ERR_INVALID, "metres_per_level must be > 0");
+        sph::mesh_scene(*s->sys, scene, verts, indices, metres_per_level);
     });
 }
 

@@ -110,10 +110,7 @@ extern "C" SPH_API int sph_density_static(const sph_params* p, int n, const floa
         if (n > SPH_STATIC_MAX_PARTICLES)
             throw Error(SPH_ERR_CAPACITY, "sph_density_static: " + std::to_string(n) + " particles exceed the fixed " +
                                               std::to_string(SPH_STATIC_MAX_PARTICLES) + "-particle scratch");
-        if (!(p->smoothing_radius > 0.0f) || !(p->cell_mult >= 0.25f) || !(p->cell_mult <= 8.0f))
-            throw Error(SPH_ERR_INVALID, "sph_density_static: bad smoothing_radius or cell_mult");
-        for (int a = 0; a < 3; ++a)
-            if (!(p->box_half[a] > 0.0f)) throw Error(SPH_ERR_INVALID, "sph_density_static: bad box_half");
+        validate_params(*p);  // the same checks as sph_scene_create
         Scene sc;
         sc.prm = *p;
         System::geometry(sc);
@@ -123,6 +120,13 @@ extern "C" SPH_API int sph_density_static(const sph_params* p, int n, const floa
                                               "-key scratch (shrink the box or raise cell_mult)");
         if (n == 0) return SPH_OK;
         cudaStream_t st = static_cast<cudaStream_t>(stream);
+        // the call ends by synchronising its stream, which a stream being
+        // captured cannot do: refuse before touching it
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+            cudaGetLastError();
+            throw Error(SPH_ERR_INVALID, "sph_density_static: the stream is being captured (the call synchronises it)");
+        }
         unsigned char* base = scratch_for_current_device();
 
         sc.n = n;

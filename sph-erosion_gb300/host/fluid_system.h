@@ -11,9 +11,20 @@
 // GetParticle returns every FluidParticle field of the last step.  Draw (an
 // OpenGL call per particle) is replaced by GetPositions, a host copy of the
 // positions for the front end's own instanced draw.
+//
+// Terrain and erosion (no counterpart in the reference, whose Run never
+// reads its Grid): SetTerrain(true) makes Run take the Grid's heightfield,
+// the dimX x dimZ block that Grid::UpdateGrid meshes, spread over the box
+// floor at metres_per_level per grey level, as the step's terrain (contact
+// with the surface); SetErosion(true) also exchanges sediment with it.  Run
+// re-uploads the heightfield whenever the Grid's heightfield or dimensions
+// change (resetting the erosion), and the Grid then shows the eroded surface
+// from UpdateGrid / GetSurfaceParts.  GetDiagnostics reads the FP64 totals
+// and the exact sediment + terrain units.
 #pragma once
 #include <cmath>
 #include <iostream>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -53,6 +64,7 @@ class FluidSystemSPH {
         check(sph_scene_create(m_sys, &p, 1024, 0, 0, &m_scene));
     }
     ~FluidSystemSPH() {
+        if (m_link) m_link->sys = nullptr;
         if (m_sys) sph_system_destroy(m_sys);
     }
     FluidSystemSPH(const FluidSystemSPH&) = delete;
@@ -66,12 +78,52 @@ class FluidSystemSPH {
         smoothRadius = h;
     }
 
-    // One simulation step (fluid_system.h:104-183).  The grid is not read by
-    // the step, exactly as in the reference.
-    void Run(Grid& /*grid*/) {
+    // One simulation step (fluid_system.h:104-183).  With the terrain off
+    // (the default) the grid is not read, exactly as in the reference; with
+    // it on, the grid's heightfield is the step's terrain.
+    void Run(Grid& grid) {
+        if (m_terrain && (m_grid_seen != &grid || m_version_seen != grid.HeightfieldVersion())) upload_terrain(grid);
         sph_params p = params();
         check(sph_scene_set_params(m_sys, m_scene, &p));
         check(sph_system_step(m_sys, 1));
+    }
+
+    // Terrain contact against the Grid's heightfield from the next Run on;
+    // metres_per_level <= 0 keeps the last scale (initially len / 255: the
+    // highest grey level reaches half the box's height).  Off removes the
+    // terrain (and stops erosion).
+    void SetTerrain(bool on, float metres_per_level = 0.0f) {
+        if (metres_per_level > 0.0f && metres_per_level != m_mpl) {
+            m_mpl = metres_per_level;
+            m_grid_seen = nullptr;  // re-upload at the new scale
+        }
+        if (!on && m_terrain) {
+            check(sph_scene_set_terrain(m_sys, m_scene, 0, 0, nullptr));
+            if (m_link) m_link->sys = nullptr;
+            m_link.reset();
+            m_grid_seen = nullptr;
+            m_erosion = false;
+        }
+        m_terrain = on;
+    }
+
+    // Sediment exchange with the terrain (turns the terrain on): capacity
+    // per m/s of speed, pickup and deposition rates (1/s) and the contact
+    // layer above the surface (<= 0: the smoothing radius).
+    void SetErosion(bool on, float k_capacity = 0.01f, float k_pickup = 5.0f, float k_deposit = 2.0f,
+                    float layer = 0.0f) {
+        if (on) SetTerrain(true);
+        m_erosion = on;
+        m_k_capacity = k_capacity;
+        m_k_pickup = k_pickup;
+        m_k_deposit = k_deposit;
+        m_layer = layer;
+    }
+
+    sph_diag GetDiagnostics() {
+        sph_diag d;
+        check(sph_scene_diag(m_sys, m_scene, &d));
+        return d;
     }
 
     std::vector<float> GetPositions() {
@@ -157,7 +209,32 @@ class FluidSystemSPH {
         p.smoothing_radius = h;
         for (int a = 0; a < 3; ++a) p.box_half[a] = len;
         p.flags = m_flags;
+        p.erosion = m_erosion ? 1 : 0;
+        p.k_capacity = m_k_capacity;
+        p.k_pickup = m_k_pickup;
+        p.k_deposit = m_k_deposit;
+        p.erosion_layer = m_layer > 0.0f ? m_layer : h;
         return p;
+    }
+
+    void upload_terrain(Grid& grid) {
+        const int w = grid.DimX(), d = grid.DimZ();
+        if (w < 2 || d < 2 || w > 512 || d > 512)
+            throw std::runtime_error("sph: the grid's dimX and dimZ must be in [2, 512] for terrain contact");
+        const float mpl = m_mpl > 0.0f ? m_mpl : len / 255.0f;
+        const std::vector<float> hts = grid.BlockHeights(mpl);
+        check(sph_scene_set_terrain(m_sys, m_scene, w, d, hts.data()));
+        if (m_link) m_link->sys = nullptr;
+        m_link = std::make_shared<sph_terrain_link>();
+        m_link->sys = m_sys;
+        m_link->scene = m_scene;
+        m_link->metres_per_level = mpl;
+        m_link->dimx = w;
+        m_link->dimz = d;
+        m_link->version = grid.HeightfieldVersion();
+        grid.Link(m_link);
+        m_grid_seen = &grid;
+        m_version_seen = grid.HeightfieldVersion();
     }
 
     void append_lattice(int n) {
@@ -185,6 +262,13 @@ class FluidSystemSPH {
 
     sph_shim::vec3 m_Origin;
     int m_flags;
+    // terrain coupling
+    bool m_terrain = false, m_erosion = false;
+    float m_mpl = 0.0f;
+    float m_k_capacity = 0.01f, m_k_pickup = 5.0f, m_k_deposit = 2.0f, m_layer = 0.0f;
+    const Grid* m_grid_seen = nullptr;
+    uint64_t m_version_seen = 0;
+    std::shared_ptr<sph_terrain_link> m_link;
     sph_system* m_sys = nullptr;
     int m_scene = -1;
 };

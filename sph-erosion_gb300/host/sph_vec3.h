@@ -6,6 +6,7 @@
 #if defined(SPH_SHIM_WITH_GLM) || (defined(__has_include) && __has_include(<glm/glm.hpp>) && \
                                    !defined(SPH_SHIM_NO_GLM))
 #include <glm/glm.hpp>
+#define SPH_SHIM_HAS_GLM 1
 namespace sph_shim {
 using vec3 = glm::vec3;
 }

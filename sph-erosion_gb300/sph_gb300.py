@@ -100,8 +100,8 @@ class ServerConfig(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("tile", C.c_int), ("cell_mult", C.c_float), ("variant", C.c_int), ("ms_per_step", C.c_float),
-                ("n_tried", C.c_int), ("tiles", C.c_int * 32), ("cell_mults", C.c_float * 32),
-                ("variants", C.c_int * 32), ("ms", C.c_float * 32)]
+                ("n_tried", C.c_int), ("tiles", C.c_int * 64), ("cell_mults", C.c_float * 64),
+                ("variants", C.c_int * 64), ("ms", C.c_float * 64)]
 
     def as_dict(self):
         return {"tile": self.tile, "cell_mult": self.cell_mult, "variant": self.variant,

@@ -52,7 +52,11 @@ int main(int argc, char** argv) {
     grid.UpdateGrid(50, 255, 50);
 
     FluidSystemSPH fluidsph(ordered ? (SPH_FLAG_RECORD | SPH_FLAG_ORDERED) : SPH_FLAG_RECORD);
+#ifdef SPH_SHIM_HAS_GLM
+    fluidsph.SetOrigin(glm::vec3(0.0));  // as Erosion/main.cpp:170
+#else
     fluidsph.SetOrigin(sph_shim::vec3(0.0f));
+#endif
     fluidsph.Initialize(1000);
     fluidsph.Run(grid);  // deltaT = 0: paused, as the front end starts
     fluidsph.SetDeltaTime(0.01f);  // the F key
@@ -71,7 +75,12 @@ int main(int argc, char** argv) {
 
     // live parameter edit through the pointer getters, then the mouse buttons
     *fluidsph.GetMass() = 0.021f;
+#ifdef SPH_SHIM_HAS_GLM
+    glm::vec3* gr = fluidsph.GetGrav();  // as Erosion/main.cpp:283-290
+    gr->y = -9.81f;
+#else
     fluidsph.GetGrav()->y = -9.81f;
+#endif
     fluidsph.Run(grid);
     fluidsph.Reset();
     fluidsph.AddParticles(125);

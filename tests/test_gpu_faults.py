@@ -122,3 +122,25 @@ def test_server_refuses_a_request_that_cannot_fit():
         (res,), stats = srv.run_trace([dict(small, arrival_s=0.0)])
     assert stats["completed"] == 1
     assert res.status == 0 and res.total_units == 0 and res.state_hash != 0
+
+
+def test_server_runs_a_request_without_lists_when_only_they_do_not_fit():
+    """With nothing resident, a request whose scene fits the budget but whose
+    neighbour lists do not is admitted and runs without the lists; it
+    completes with status 0, exact mass and the same fingerprint as with the
+    lists (the per-lane passes give the same bits either way), and the next
+    request is admitted only once it has retired."""
+    a = dict(seed=7011, particles=40000, terrain_side=128, steps=24)
+    b = dict(seed=7012, particles=2048, terrain_side=64, steps=12)
+    with S.Server(W.base_params(), chunk_steps=8) as roomy:
+        (ra_lists,), st = roomy.run_trace([dict(a, arrival_s=0.0)])
+    # the lists are 516 B per particle of the particle arena (at least 2^16
+    # particles: 33.8 MB); a budget 16 MB under the peak holds everything else
+    budget = int(st["peak_bytes"]) - (16 << 20)
+    with S.Server(W.base_params(), chunk_steps=8, hbm_budget=budget) as srv:
+        (ra, rb), stats = srv.run_trace([dict(a, arrival_s=0.0), dict(b, arrival_s=0.0)])
+    assert stats["peak_bytes"] <= budget
+    assert ra.status == 0 and rb.status == 0
+    assert ra.total_units == 0 and rb.total_units == 0 and ra.nan_particles == 0
+    assert ra.state_hash == ra_lists.state_hash
+    assert rb.admit_s >= ra.done_s  # b waited for a to retire

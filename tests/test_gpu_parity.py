@@ -237,6 +237,51 @@ def test_kernel_variants_identical(golden, cell_mult):
             assert np.array_equal(got[s][1], base[s][1]), (v, s)
 
 
+# The cooperative variants (a group of lanes per particle): 32 density
+# lanes and 8 force lanes (264), relaxed force registers (268), packed
+# records (392), 4 and 16 force lanes (776, 1288), 16 density lanes (2312).
+COOP = (264, 268, 392, 776, 1288, 2312)
+
+
+@pytest.mark.parametrize("cell_mult", [1.0, 0.5])
+def test_cooperative_variants_within_tolerance(golden, cell_mult):
+    """The cooperative passes sum each particle's terms in another order
+    (per-lane partial sums combined by a fixed shuffle tree), so they are
+    held to RTOL, not to the bits of the per-lane passes: every field within
+    RTOL of the reference after 1 step and of the per-lane passes after 30,
+    NeighbId equal after 1 step.  They are deterministic: graphs or eager
+    launches and either tile size give the same bits."""
+    g = golden("ref_c1_2048.npz")
+    base = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=88)
+    for v in COOP:
+        got = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=v)
+        e1 = field_errors(got[1][0], g["rec1"])
+        e30 = field_errors(got[30][0], base[30][0])
+        _report(f"variant {v} cell_mult {cell_mult} step 1 vs reference", e1)
+        _report(f"variant {v} cell_mult {cell_mult} step 30 vs variant 88", e30)
+        assert max(e1.values()) <= RTOL, v
+        assert np.array_equal(got[1][1], g["nb1"]), v
+        assert max(e30.values()) <= RTOL, v
+    a = run(C1, g["pos0"], 30, cell_mult=cell_mult, variant=264, graph_steps=16, tile=256)[30]
+    b = run(C1, g["pos0"], 30, cell_mult=cell_mult, variant=264, graph_steps=0, tile=128)[30]
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_cooperative_overflow_path():
+    """Particles with more in-range neighbours than a list holds: the
+    cooperative force pass splits their cell rows over the group instead;
+    within RTOL of the per-lane passes after one step."""
+    rng = np.random.default_rng(5)
+    blob = rng.uniform(-0.006, 0.006, (300, 3))
+    lattice = np.stack(np.meshgrid(*[np.arange(-0.18, 0.18, 0.024)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    pos = np.concatenate([blob, lattice[np.abs(lattice).max(1) > 0.05]]).astype(np.float32)
+    a = run(REF, pos, 1, variant=0)[1]
+    for v in (264, 776, 1288):
+        b = run(REF, pos, 1, variant=v)[1]
+        assert max(field_errors(b[0], a[0]).values()) <= RTOL, v
+        assert np.array_equal(a[1], b[1]), v
+
+
 def test_neighbour_list_overflow_falls_back_exactly():
     """Particles with more in-range neighbours than a list holds (64) make
     their warp traverse the cells again: same bits as without lists."""

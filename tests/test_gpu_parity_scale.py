@@ -52,7 +52,9 @@ def _sample_check(O, op, st, base, delta, nb_prev, rec, nb, sed, ids, tag):
     assert ds.max() <= 1 + RTOL * max(1, np.abs(o["sed"]).max()), (tag, ds.max())
 
 
-def test_plain_1m_sampled_fields_vs_oracle(oracle_lib):
+@pytest.mark.parametrize("variant", [88, 264])
+def test_plain_1m_sampled_fields_vs_oracle(oracle_lib, variant):
+    """Per-lane passes (88) and cooperative passes (264)."""
     import workloads as W
 
     O = oracle_lib
@@ -61,7 +63,7 @@ def test_plain_1m_sampled_fields_vs_oracle(oracle_lib):
     t = spec["terrain"]
     op = oracle_params(O, spec["params"], terrain=(t["w"], t["d"]))
     ids = np.sort(np.random.default_rng(42).choice(n, SAMPLE, replace=False)).astype(np.int32)
-    with S.System(particle_capacity=n, key_capacity=1 << 20, terrain_capacity=1 << 21) as sysm:
+    with S.System(particle_capacity=n, key_capacity=1 << 20, terrain_capacity=1 << 21, variant=variant) as sysm:
         sc = W.build_scene(sysm, spec, flags=S.SPH_FLAG_RECORD)
         base, delta = sc.get_terrain()  # no erosion yet: the heights are the base
         assert not delta.any()
@@ -69,7 +71,7 @@ def test_plain_1m_sampled_fields_vs_oracle(oracle_lib):
         sysm.step(1)
         rec, nb = sc.get_records()
         _sample_check(O, op, st, base, delta, np.full(n, -1, np.int32), rec, nb, sc.get_particles()["sed"], ids,
-                      "1M step 1")
+                      f"1M variant {variant} step 1")
         sysm.step(299)
         st = sc.get_particles()
         _, delta = sc.get_terrain()
@@ -77,7 +79,7 @@ def test_plain_1m_sampled_fields_vs_oracle(oracle_lib):
         sysm.step(1)
         rec, nb = sc.get_records()
         after = sc.get_particles()
-        _sample_check(O, op, st, base, delta, nb_prev, rec, nb, after["sed"], ids, "1M step 301")
+        _sample_check(O, op, st, base, delta, nb_prev, rec, nb, after["sed"], ids, f"1M variant {variant} step 301")
         assert sc.diag()["total_units"] == 0
         # the developed state is past the lattice: the sample's neighbourhoods differ
         cnt = sc.neighbour_counts()[ids]

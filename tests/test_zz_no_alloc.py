@@ -32,7 +32,7 @@ def _scene_density(params, pos):
 
 
 def _static_density(params, pos):
-    torch = pytest.importorskip("torch")
+    import torch  # the caller-side buffers: a GPU run without torch fails here instead of skipping
     dev_pos = torch.from_numpy(np.ascontiguousarray(pos, np.float32).ravel()).cuda()
     dens = torch.full((len(pos),), -1.0, dtype=torch.float32, device="cuda")
     pres = torch.full((len(pos),), -1.0, dtype=torch.float32, device="cuda")
@@ -68,3 +68,27 @@ def test_static_density_rejects_oversize():
     big = S.default_params(**dict(C1, box_half=(2.0, 2.0, 2.0)))  # 100^3 cells: 1.6M keys
     assert S.lib().sph_density_static(C.byref(big), 10, C.c_void_p(1), C.c_void_p(1), None, None) == -4
     assert b"keys" in S.lib().sph_last_error()
+
+
+def test_static_density_refuses_a_capturing_stream():
+    """Every call ends by synchronising its stream, which a stream being
+    captured into a CUDA graph cannot do: on such a stream the call returns
+    SPH_ERR_INVALID before touching it, and the capture stays usable."""
+    import torch
+
+    params = S.default_params(**C1)
+    pos = torch.zeros(30, dtype=torch.float32, device="cuda")
+    dens = torch.zeros(10, dtype=torch.float32, device="cuda")
+    x = torch.zeros(1, dtype=torch.float32, device="cuda")
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side):
+        x.add_(1.0)
+        rc = S.lib().sph_density_static(C.byref(params), 10, C.c_void_p(pos.data_ptr()), C.c_void_p(dens.data_ptr()),
+                                        None, C.c_void_p(side.cuda_stream))
+    assert rc == -1
+    assert b"captured" in S.lib().sph_last_error()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert x.item() == 1.0
