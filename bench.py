@@ -81,9 +81,10 @@ def source_digest() -> str:
 
 
 # The variant bits that select the force kernel (4 register budget, 8 lists,
-# 16 list walk loaded ahead, 128 packed records); the others change only the
-# density pass, whose lists are the same in every variant.
-FORCE_BITS = 4 | 8 | 16 | 128
+# 16 list walk loaded ahead, 128 packed records, 256 cooperative pass with
+# 512/1024 its group size, 32768 dynamically scheduled warp slices); the
+# others change only the density pass.
+FORCE_BITS = 4 | 8 | 16 | 128 | 256 | 512 | 1024 | 32768
 
 
 def ncu_counters(workload, variant, cm):
@@ -307,12 +308,21 @@ def calibration_keys():
 def traversal(scene, step_ms):
     """Neighbour-search counters at the end of the run: per particle, the
     candidates each of the two neighbour passes tests and the in-range pairs
-    it evaluates; pair tests per second over the whole step."""
+    it evaluates; pair tests per second over the whole step; the spread of
+    in-range neighbour counts and the share of particles whose list (128
+    entries, self included) overflows, and of 32-particle warps holding one."""
     t = scene.traversal_stats()
     n = max(t["particles"], 1)
+    cnt = scene.neighbour_counts()  # by id; warps hold sorted order
+    _, order = scene.debug_sort()
+    c = cnt[order] + 1
+    over = c > 128
+    warps = over[: len(over) // 32 * 32].reshape(-1, 32).any(axis=1) if len(over) >= 32 else over
     return {"candidates_per_particle": t["candidates"] / n, "in_range_per_particle": t["in_range"] / n,
             "rows_per_particle": t["rows"] / n, "pair_tests_per_s": 2 * t["candidates"] / (step_ms * 1e-3),
             "in_range_pairs_per_s": 2 * t["in_range"] / (step_ms * 1e-3),
+            "in_range_percentiles": {str(q): int(np.percentile(c, q)) for q in (50, 90, 99, 99.9, 100)},
+            "list_overflow_frac": float(over.mean()), "warps_with_overflow_frac": float(warps.mean()),
             "reference_pair_tests_per_step": 3 * n * n}
 
 

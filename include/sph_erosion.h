@@ -127,7 +127,10 @@ typedef struct sph_system_config {
                                      particle: the density pass sweeps the particle's
                                      candidates 32 at a time (2048: 16 lanes), the force
                                      pass splits its list over 8 lanes (512: 4, 1024: 16);
-                                     with 256, bit 4 relaxes the force pass's registers;
+                                     with 256, bit 4 relaxes the force pass's registers,
+                             32768 = with 8 + 16: the force pass's warps take their work
+                                     in 32-particle slices from a counter instead of one
+                                     block per tile (65536: the density pass's); same bits;
                                 default 88 (8 + 16 + 64) */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;

@@ -196,7 +196,8 @@ System::System(const sph_system_config& cfg) : cfg_(cfg) {
     steps_.resize(cfg_.max_scenes, false, st_);
     nwork_.resize(4, false, st_);
     slist_.resize(cfg_.max_scenes, false, st_);
-    status_.resize(1, false, st_);
+    status_.resize(3, false, st_);  // status word + the two work counters
+    SPH_CK(cudaMemsetAsync(status_.p, 0, 3 * sizeof(unsigned), st_));
     diag_part_.resize((int64_t)kDiagBlocks * kDiagDoubles, false, st_);
     diag_i_.resize(3, false, st_);
     diag_nan_.resize(1, false, st_);
@@ -1101,6 +1102,8 @@ DevArrays System::arrays() const {
     a.tdelta = tdelta_.p;
     a.theight = theight_.p;
     a.status = status_.p;
+    a.ctr = status_.p + 1;
+    a.tile = cfg_.tile;
     return a;
 }
 
@@ -1111,6 +1114,10 @@ LaunchShape System::shape() const {
     s.grid_c = n_ctiles_;
     s.grid_t = n_ttiles_;
     s.variant = nl_ready_ ? cfg_.variant : (cfg_.variant & ~504);
+    // enough blocks to fill every SM (2048 threads each); blocks that start
+    // after the counter ran out exit at once
+    const int64_t slices = (int64_t)n_ptiles_ * (cfg_.tile / 32);
+    s.grid_dyn = (int)std::min<int64_t>((slices * 32 + cfg_.tile - 1) / cfg_.tile, (int64_t)nsm_ * (2048 / cfg_.tile));
     return s;
 }
 
@@ -1385,11 +1392,12 @@ void System::autotune(int steps, sph_tune_result* out) {
     };
     const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
-    // per-lane passes (0, 4: cells; 28, 88, 120, 216: lists) and cooperative
+    // per-lane passes (0, 4: cells; 28, 88, 120, 216: lists; 32856, 32888:
+    // the force pass in dynamically scheduled warp slices) and cooperative
     // passes (264: 32 + 8 lanes per particle, 268 with relaxed force
     // registers, 392 packed records, 776 and 1288: 4 and 16 force lanes,
     // 2312: 16 density lanes)
-    const int variants[] = {0, 4, 28, 88, 120, 216, 264, 268, 392, 776, 1288, 2312};
+    const int variants[] = {0, 4, 28, 88, 120, 216, 32856, 32888, 264, 268, 392, 776, 1288, 2312};
     static_assert(2 * 2 * (sizeof variants / sizeof variants[0]) <= 64, "sph_tune_result holds 64 trials");
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;

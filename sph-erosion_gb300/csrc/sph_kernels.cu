@@ -648,6 +648,7 @@ __global__ void __launch_bounds__(kMaxTile) k_scatter(DevArrays a) {
 // the sorted arrays.
 __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
     const int nwork = *a.n_ptiles;
+    if (a.ctr && blockIdx.x == 0 && threadIdx.x < 2) a.ctr[threadIdx.x] = 0u;  // for this step's neighbour kernels
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = a.ptiles[w];
         if (a.steps_left[wk.scene] == 0) continue;
@@ -676,21 +677,44 @@ __global__ void __launch_bounds__(kMaxTile) k_reorder(DevArrays a) {
     }
 }
 
+// Work slices of the neighbour kernels.  Static: block b takes the tiles b,
+// b + gridDim.x, ..., and its thread t the tile's lane t.  Dynamic (DYN):
+// every warp takes the next 32-lane slice of any tile from a counter, so no
+// warp slot waits for the slowest warp of its block.  Which warp computes a
+// particle changes nothing in what it computes.
+template <bool DYN>
+__device__ __forceinline__ int next_slice(unsigned* ctr, int cur) {
+    if (!DYN) return cur + (int)gridDim.x;
+    int t = 0;
+    if ((threadIdx.x & 31) == 0) t = (int)atomicAdd(ctr, 1u);
+    return __shfl_sync(kFull, t, 0);
+}
+
+template <bool DYN>
+__device__ __forceinline__ int first_slice(unsigned* ctr) {
+    return DYN ? next_slice<true>(ctr, 0) : (int)blockIdx.x;
+}
+
 // density: pass 1 (fluid_system.h:107-124), then the per-particle factors the
 // force pass reuses: P/rho^2 and m/rho.
 // LISTED: the in-range pairs are compacted (for_each_in_range_listed) instead
 // of evaluated inside the candidate loop; which one is faster depends on the
 // neighbour density, so the autotuner picks it.
-template <bool ORDERED, bool LISTED, int MINB, bool NL = false, bool X2 = false, bool PACK = false>
+template <bool ORDERED, bool LISTED, int MINB, bool NL = false, bool X2 = false, bool PACK = false,
+          bool DYN = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
-    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int spt = DYN ? a.tile / 32 : 1;  // slices per tile
+    for (int sl = first_slice<DYN>(a.ctr); sl < nwork * spt; sl = next_slice<DYN>(a.ctr, sl)) {
+        const int w = DYN ? sl / spt : sl;
+        const int li = DYN ? (sl % spt) * 32 + (int)(threadIdx.x & 31) : (int)threadIdx.x;  // lane within the tile
+        const int stride = DYN ? a.tile : (int)blockDim.x;
         const Work wk = a.ptiles[w];
         if (a.steps_left[wk.scene] == 0) continue;
         const SceneDev S = a.scenes[wk.scene];  // by value: the list stores cannot alias it
         if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
-        const int p = wk.start + threadIdx.x;
+        const int p = wk.start + li;
         const bool valid = p < S.p_off + S.n;
         if ((ORDERED || !LISTED) && !valid) continue;
         const float4 xi = a.spos[valid ? p : S.p_off];
@@ -712,14 +736,14 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
         } else {
             // NL: the in-range candidates, in visiting order, also go to the
             // particle's neighbour list for the force pass
-            uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
+            uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + li;
             int cnt = 0;
             auto visit = [&](uint32_t j, float4 xj) {
                 const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
                 if (s <= S.smax) {
                     rho = fa(rho, density_term(S, fsq(s)));
                     if (NL) {
-                        if (cnt < kNbCap) nl[(size_t)cnt * blockDim.x] = j;
+                        if (cnt < kNbCap) nl[(size_t)cnt * stride] = j;
                         ++cnt;
                     }
                 }
@@ -844,16 +868,20 @@ __device__ __forceinline__ void integrate_and_store(const DevArrays& a, const Sc
 // overflowed walks its cells instead.  NL = 2
 // software-pipelines the list walk: list entries two ahead and the
 // neighbour's state one ahead are loaded before the current pair is summed.
-template <bool ORDERED, int MINB, int NL = 0>
+template <bool ORDERED, int MINB, int NL = 0, bool DYN = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
-    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int spt = DYN ? a.tile / 32 : 1;  // slices per tile
+    for (int sl = first_slice<DYN>(a.ctr + 1); sl < nwork * spt; sl = next_slice<DYN>(a.ctr + 1, sl)) {
+        const int w = DYN ? sl / spt : sl;
+        const int li = DYN ? (sl % spt) * 32 + (int)(threadIdx.x & 31) : (int)threadIdx.x;  // lane within the tile
+        const int lstride = DYN ? a.tile : (int)blockDim.x;
         const Work wk = a.ptiles[w];
         if (a.steps_left[wk.scene] == 0) continue;
         const SceneDev& S = a.scenes[wk.scene];
         if (((S.flags & kFlagOrdered) != 0) != ORDERED) continue;
-        const int p0 = wk.start + threadIdx.x;
+        const int p0 = wk.start + li;
         const bool valid = p0 < S.p_off + S.n;
         if (ORDERED && !valid) continue;
         const int p = valid ? p0 : S.p_off;
@@ -886,14 +914,14 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
                     if (dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z)) <= S.smax) pair(j, xj);
                 });
             } else if (NL == 1) {
-                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
+                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + li;
                 for (int q = 0; q < cnt; ++q) {
-                    const uint32_t j = __ldg(nl + (size_t)q * blockDim.x);
+                    const uint32_t j = __ldg(nl + (size_t)q * lstride);
                     pair(j, __ldg(sp + j));
                 }
             } else if (NL == 2) {
-                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
-                const int stride = blockDim.x;
+                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + li;
+                const int stride = lstride;
                 uint32_t j0 = cnt > 0 ? __ldg(nl) : 0u;
                 uint32_t j1 = cnt > 1 ? __ldg(nl + stride) : 0u;
                 float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), v0 = x0, d0 = x0;
@@ -921,8 +949,8 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
             } else {
                 // NL == 3: the same walk over the packed 32-byte records (one
                 // sector per neighbour); the id is read only in record mode
-                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + threadIdx.x;
-                const int stride = blockDim.x;
+                const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap + li;
+                const int stride = lstride;
                 const float4* fd = a.fdat + 2 * (size_t)S.p_off;
                 const bool rec = (S.flags & kFlagRecord) != 0;
                 uint32_t j0 = cnt > 0 ? __ldg(nl) : 0u;
@@ -1434,17 +1462,28 @@ static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.til
 // budget alone (4 resident blocks of 256 threads); bit 6 pairs the density pass's
 // candidate loads; bit 7 with bit 3 packs each particle's force-pass inputs
 // into one 32-byte record.
+template <int MINB, bool DYN>
+static void launch_density_nl_d(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
+    const bool x2 = (s.variant & 64) != 0, pack = (s.variant & 128) != 0;
+    const int grid = DYN ? s.grid_dyn : s.grid_p;
+    if (x2 && pack)
+        k_density<false, false, MINB, true, true, true, DYN><<<grid, s.tile, 0, st>>>(a);
+    else if (x2)
+        k_density<false, false, MINB, true, true, false, DYN><<<grid, s.tile, 0, st>>>(a);
+    else if (pack)
+        k_density<false, false, MINB, true, false, true, DYN><<<grid, s.tile, 0, st>>>(a);
+    else
+        k_density<false, false, MINB, true, false, false, DYN><<<grid, s.tile, 0, st>>>(a);
+}
+
+// Bit 16 (65536): the list-writing density pass takes its work in warp
+// slices from a counter (dynamic scheduling; same bits).
 template <int MINB>
 static void launch_density_nl(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    const bool x2 = (s.variant & 64) != 0, pack = (s.variant & 128) != 0;
-    if (x2 && pack)
-        k_density<false, false, MINB, true, true, true><<<s.grid_p, s.tile, 0, st>>>(a);
-    else if (x2)
-        k_density<false, false, MINB, true, true, false><<<s.grid_p, s.tile, 0, st>>>(a);
-    else if (pack)
-        k_density<false, false, MINB, true, false, true><<<s.grid_p, s.tile, 0, st>>>(a);
+    if (s.variant & 65536)
+        launch_density_nl_d<MINB, true>(a, s, st);
     else
-        k_density<false, false, MINB, true, false, false><<<s.grid_p, s.tile, 0, st>>>(a);
+        launch_density_nl_d<MINB, false>(a, s, st);
 }
 
 // Variant bit 8 (with bit 3): the cooperative passes, G lanes per particle.
@@ -1533,14 +1572,26 @@ void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
         return;
     }
     // the list variants walk their lists (or, on overflow, the cells) per
-    // lane and need no shared memory
+    // lane and need no shared memory; bit 15 (32768) has the pipelined list
+    // walks take their work in warp slices from a counter (same bits)
+    const bool dyn = (s.variant & 32768) != 0;
     if ((s.variant & 136) == 136) {
-        if (s.variant & 4)
+        if (dyn) {
+            if (s.variant & 4)
+                k_force<false, 3, 3, true><<<s.grid_dyn, s.tile, 0, st>>>(a);
+            else
+                k_force<false, 4, 3, true><<<s.grid_dyn, s.tile, 0, st>>>(a);
+        } else if (s.variant & 4)
             k_force<false, 3, 3><<<s.grid_p, s.tile, 0, st>>>(a);
         else
             k_force<false, 4, 3><<<s.grid_p, s.tile, 0, st>>>(a);
     } else if ((s.variant & 24) == 24) {
-        if (s.variant & 4)
+        if (dyn) {
+            if (s.variant & 4)
+                k_force<false, 3, 2, true><<<s.grid_dyn, s.tile, 0, st>>>(a);
+            else
+                k_force<false, 4, 2, true><<<s.grid_dyn, s.tile, 0, st>>>(a);
+        } else if (s.variant & 4)
             k_force<false, 3, 2><<<s.grid_p, s.tile, 0, st>>>(a);
         else
             k_force<false, 4, 2><<<s.grid_p, s.tile, 0, st>>>(a);

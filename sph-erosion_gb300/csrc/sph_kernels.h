@@ -53,6 +53,11 @@ struct DevArrays {
     float4* fdat;
     // status word: bit 0 = ordered-mode neighbour overflow
     unsigned* status;
+    // work counters of the dynamically scheduled neighbour kernels
+    // ([0] density, [1] force), cleared by the reorder kernel every step;
+    // null where no kernel is scheduled that way
+    unsigned* ctr;
+    int tile;      // lanes per work tile (the list stride)
 };
 
 // Slots per particle of the in-range neighbour lists.
@@ -64,6 +69,7 @@ struct LaunchShape {
     int grid_c;      // persistent grid of the scan
     int grid_t;      // persistent grid of the terrain kernel
     int variant;     // sph_system_config.variant bits (bit 3 only with lists allocated)
+    int grid_dyn;    // grid of the dynamically scheduled neighbour kernels
 };
 
 // Once per process and device: opt the list-traversal kernels into >48 KB of

@@ -225,12 +225,13 @@ def test_kernel_variants_identical(golden, cell_mult):
     """Every kernel variant visits the in-range neighbours in the same order:
     compacted density lists (1), relaxed registers (4), neighbour lists
     handed from the density to the force pass (8, 12), walked with loads
-    ahead (24, 28, 56), with paired candidate loads (88) and over packed
-    neighbour records (152, 216) give the same bits as the cell traversal in
-    both passes (0), records and NeighbId included."""
+    ahead (24, 28, 56), with paired candidate loads (88), over packed
+    neighbour records (152, 216) and with the work taken in warp slices from
+    a counter (32856, 65624, 98392, 98520) give the same bits as the cell
+    traversal in both passes (0), records and NeighbId included."""
     g = golden("ref_c1_2048.npz")
     base = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=0)
-    for v in (1, 4, 8, 12, 24, 28, 56, 88, 152, 216):
+    for v in (1, 4, 8, 12, 24, 28, 56, 88, 152, 216, 32856, 65624, 98392, 98520):
         got = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=v)
         for s in (1, 30):
             assert np.array_equal(got[s][0], base[s][0]), (v, s)
