@@ -130,7 +130,12 @@ typedef struct sph_system_config {
                                      with 256, bit 4 relaxes the force pass's registers,
                              32768 = with 8 + 16: the force pass's warps take their work
                                      in 32-particle slices from a counter instead of one
-                                     block per tile (65536: the density pass's); same bits;
+                                     block per tile (65536: the density pass's); same bits,
+                            131072 = with 8 + 16: fast arithmetic in both neighbour passes
+                                     (grouped products, fused multiply-adds, r^2 for
+                                     |r|^2, hardware 1/sqrt); exact in-range test, so the
+                                     neighbour sets and NeighbId are unchanged, but not
+                                     the reference's rounding (within the 1e-4 bar);
                                 default 88 (8 + 16 + 64) */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;

@@ -1393,11 +1393,12 @@ void System::autotune(int steps, sph_tune_result* out) {
     const int tiles[2] = {128, 256};
     const float cms[2] = {1.0f, 0.5f};
     // per-lane passes (0, 4: cells; 28, 88, 120, 216: lists; 32856, 32888:
-    // the force pass in dynamically scheduled warp slices) and cooperative
-    // passes (264: 32 + 8 lanes per particle, 268 with relaxed force
-    // registers, 392 packed records, 776 and 1288: 4 and 16 force lanes,
-    // 2312: 16 density lanes)
-    const int variants[] = {0, 4, 28, 88, 120, 216, 32856, 32888, 264, 268, 392, 776, 1288, 2312};
+    // the force pass in dynamically scheduled warp slices; 163928, 163960,
+    // 164088: the same in fast arithmetic, 164088 with packed records) and
+    // cooperative passes (264: 32 + 8 lanes per particle, 776: 4 force
+    // lanes, 2312: 16 density lanes)
+    const int variants[] = {0,     4,      28,     88,     120, 216, 32856, 32888,
+                            163928, 163960, 164088, 264,    776, 2312};
     static_assert(2 * 2 * (sizeof variants / sizeof variants[0]) <= 64, "sph_tune_result holds 64 trials");
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;

@@ -384,6 +384,56 @@ __device__ __forceinline__ void force_pair(const SceneDev& S, ForceAcc& acc, flo
     acc.nz = fa(acc.nz, fm(Bj, -fm(fm(rz, S.c_grad), pw)));
 }
 
+// Fast-arithmetic form of density_term and force_pair (variant bit 17, fast
+// mode only): the same kernel terms with the products grouped, fused
+// multiply-adds, r^2 in place of |r|^2 and a hardware reciprocal square root
+// for 1/|r|.  The in-range test stays exact (s <= smax), so the neighbour sets
+// and NeighbId are the reference's; the rounding is not, and the results are
+// held to the parity tolerance instead of to bits.
+__device__ __forceinline__ float density_term_fast(const SceneDev& S, float s) {
+    const float hs = S.hh - s;
+    return (S.mass * S.c_poly6) * (hs * hs * hs);
+}
+
+__device__ __forceinline__ void force_pair_fast(const SceneDev& S, ForceAcc& acc, float rx, float ry, float rz,
+                                                float s, float vix, float viy, float viz, float Ai, float4 vj,
+                                                float Aj, float Bj, int idj, bool self) {
+    const float hs = S.hh - s;  // h^2 - r^2
+    // pass 3: colour-field Laplacian, self included (laplDefault)
+    acc.cfl = fmaf(Bj, (-S.c_grad * hs) * fmaf(-7.0f, s, 3.0f * S.hh), acc.cfl);
+    if (self) return;
+    acc.nb = max(acc.nb, idj);
+    acc.any = 1;
+    const float coef = (Ai + Aj) * S.mass;
+    if (s < S.cthr * S.cthr) {
+        // coincident: gradPressure along normalize(1, 1, 1)
+        const float hl = S.h - sqrtf(s);
+        const float g = -(S.inv_sqrt3 * S.c_spiky) * (hl * hl) * coef;
+        acc.fpx += g;
+        acc.fpy += g;
+        acc.fpz += g;
+        const float bl = Bj * (S.c_spiky * hl);
+        acc.fvx = fmaf(vj.x - vix, bl, acc.fvx);
+        acc.fvy = fmaf(vj.y - viy, bl, acc.fvy);
+        acc.fvz = fmaf(vj.z - viz, bl, acc.fvz);
+    } else {
+        const float inv = rsqrtf(s);  // 1/|r|
+        const float hl = S.h - s * inv;  // h - |r|
+        const float g = -(S.c_spiky * coef) * (hl * hl) * inv;  // gradPressure / |r|, times coef
+        acc.fpx = fmaf(rx, g, acc.fpx);
+        acc.fpy = fmaf(ry, g, acc.fpy);
+        acc.fpz = fmaf(rz, g, acc.fpz);
+        const float bl = Bj * (S.c_spiky * hl);  // laplVisc times m/rho_j
+        acc.fvx = fmaf(vj.x - vix, bl, acc.fvx);
+        acc.fvy = fmaf(vj.y - viy, bl, acc.fvy);
+        acc.fvz = fmaf(vj.z - viz, bl, acc.fvz);
+    }
+    const float gn = -(Bj * S.c_grad) * (hs * hs);  // gradDefault / r, times m/rho_j
+    acc.nx = fmaf(rx, gn, acc.nx);
+    acc.ny = fmaf(ry, gn, acc.ny);
+    acc.nz = fmaf(rz, gn, acc.nz);
+}
+
 struct TSample {
     float y;
     float nx, ny, nz;
@@ -701,7 +751,7 @@ __device__ __forceinline__ int first_slice(unsigned* ctr) {
 // of evaluated inside the candidate loop; which one is faster depends on the
 // neighbour density, so the autotuner picks it.
 template <bool ORDERED, bool LISTED, int MINB, bool NL = false, bool X2 = false, bool PACK = false,
-          bool DYN = false>
+          bool DYN = false, bool FM = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
@@ -741,7 +791,10 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_density(DevArrays a) {
             auto visit = [&](uint32_t j, float4 xj) {
                 const float s = dist2(fs(xi.x, xj.x), fs(xi.y, xj.y), fs(xi.z, xj.z));
                 if (s <= S.smax) {
-                    rho = fa(rho, density_term(S, fsq(s)));
+                    if (FM)
+                        rho += density_term_fast(S, s);
+                    else
+                        rho = fa(rho, density_term(S, fsq(s)));
                     if (NL) {
                         if (cnt < kNbCap) nl[(size_t)cnt * stride] = j;
                         ++cnt;
@@ -868,7 +921,7 @@ __device__ __forceinline__ void integrate_and_store(const DevArrays& a, const Sc
 // overflowed walks its cells instead.  NL = 2
 // software-pipelines the list walk: list entries two ahead and the
 // neighbour's state one ahead are loaded before the current pair is summed.
-template <bool ORDERED, int MINB, int NL = 0, bool DYN = false>
+template <bool ORDERED, int MINB, int NL = 0, bool DYN = false, bool FM = false>
 __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
     extern __shared__ uint32_t list[];
     const int nwork = *a.n_ptiles;
@@ -897,8 +950,12 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
         auto pair_with = [&](uint32_t j, float4 xj, float4 vj, float4 dj) {
             const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
             const float s = dist2(rx, ry, rz);
-            force_pair(S, acc, rx, ry, rz, fsq(s), vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z, __float_as_int(xj.w),
-                       (int)j == pl);
+            if (FM)
+                force_pair_fast(S, acc, rx, ry, rz, s, vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z, __float_as_int(xj.w),
+                                (int)j == pl);
+            else
+                force_pair(S, acc, rx, ry, rz, fsq(s), vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z, __float_as_int(xj.w),
+                           (int)j == pl);
         };
         auto pair = [&](uint32_t j, float4 xj) { pair_with(j, xj, __ldg(sv + j), __ldg(sd + j)); };
         if (ORDERED) {
@@ -970,8 +1027,12 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
                     }
                     const int idj = rec ? __float_as_int(__ldg(&sp[j0].w)) : 0;
                     const float rx = fs(xi.x, a0.x), ry = fs(xi.y, a0.y), rz = fs(xi.z, a0.z);
-                    force_pair(S, acc, rx, ry, rz, fsq(dist2(rx, ry, rz)), vi.x, vi.y, vi.z, Ai, b0, a0.w, b0.w, idj,
-                               (int)j0 == pl);
+                    if (FM)
+                        force_pair_fast(S, acc, rx, ry, rz, dist2(rx, ry, rz), vi.x, vi.y, vi.z, Ai, b0, a0.w, b0.w,
+                                        idj, (int)j0 == pl);
+                    else
+                        force_pair(S, acc, rx, ry, rz, fsq(dist2(rx, ry, rz)), vi.x, vi.y, vi.z, Ai, b0, a0.w, b0.w,
+                                   idj, (int)j0 == pl);
                     j0 = j1;
                     j1 = j2;
                     a0 = a1;
@@ -1462,28 +1523,35 @@ static size_t list_bytes(const LaunchShape& s) { return (size_t)kListCap * s.til
 // budget alone (4 resident blocks of 256 threads); bit 6 pairs the density pass's
 // candidate loads; bit 7 with bit 3 packs each particle's force-pass inputs
 // into one 32-byte record.
-template <int MINB, bool DYN>
+template <int MINB, bool DYN, bool FM>
 static void launch_density_nl_d(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     const bool x2 = (s.variant & 64) != 0, pack = (s.variant & 128) != 0;
     const int grid = DYN ? s.grid_dyn : s.grid_p;
     if (x2 && pack)
-        k_density<false, false, MINB, true, true, true, DYN><<<grid, s.tile, 0, st>>>(a);
+        k_density<false, false, MINB, true, true, true, DYN, FM><<<grid, s.tile, 0, st>>>(a);
     else if (x2)
-        k_density<false, false, MINB, true, true, false, DYN><<<grid, s.tile, 0, st>>>(a);
+        k_density<false, false, MINB, true, true, false, DYN, FM><<<grid, s.tile, 0, st>>>(a);
     else if (pack)
-        k_density<false, false, MINB, true, false, true, DYN><<<grid, s.tile, 0, st>>>(a);
+        k_density<false, false, MINB, true, false, true, DYN, FM><<<grid, s.tile, 0, st>>>(a);
     else
-        k_density<false, false, MINB, true, false, false, DYN><<<grid, s.tile, 0, st>>>(a);
+        k_density<false, false, MINB, true, false, false, DYN, FM><<<grid, s.tile, 0, st>>>(a);
 }
 
 // Bit 16 (65536): the list-writing density pass takes its work in warp
-// slices from a counter (dynamic scheduling; same bits).
+// slices from a counter (dynamic scheduling; same bits).  Bit 17 (131072):
+// fast arithmetic (density_term_fast; not the same bits).
 template <int MINB>
 static void launch_density_nl(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    if (s.variant & 65536)
-        launch_density_nl_d<MINB, true>(a, s, st);
+    const bool fm = (s.variant & 131072) != 0;
+    if (s.variant & 65536) {
+        if (fm)
+            launch_density_nl_d<MINB, true, true>(a, s, st);
+        else
+            launch_density_nl_d<MINB, true, false>(a, s, st);
+    } else if (fm)
+        launch_density_nl_d<MINB, false, true>(a, s, st);
     else
-        launch_density_nl_d<MINB, false>(a, s, st);
+        launch_density_nl_d<MINB, false, false>(a, s, st);
 }
 
 // Variant bit 8 (with bit 3): the cooperative passes, G lanes per particle.
@@ -1575,6 +1643,20 @@ void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     // lane and need no shared memory; bit 15 (32768) has the pipelined list
     // walks take their work in warp slices from a counter (same bits)
     const bool dyn = (s.variant & 32768) != 0;
+    if ((s.variant & 131072) && (s.variant & 24) == 24) {
+        // bit 17: fast arithmetic (force_pair_fast), pipelined list walk
+        const bool pack = (s.variant & 128) != 0;
+        if (pack) {
+            if (dyn)
+                k_force<false, 4, 3, true, true><<<s.grid_dyn, s.tile, 0, st>>>(a);
+            else
+                k_force<false, 4, 3, false, true><<<s.grid_p, s.tile, 0, st>>>(a);
+        } else if (dyn)
+            k_force<false, 4, 2, true, true><<<s.grid_dyn, s.tile, 0, st>>>(a);
+        else
+            k_force<false, 4, 2, false, true><<<s.grid_p, s.tile, 0, st>>>(a);
+        return;
+    }
     if ((s.variant & 136) == 136) {
         if (dyn) {
             if (s.variant & 4)

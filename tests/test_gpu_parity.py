@@ -112,10 +112,13 @@ def test_plain_2048_parity(oracle_lib, golden, ordered):
 POWF_RESIDUAL_2048 = {"acc": 1.36e-4, "fpress": 1.25e-4}
 
 
-def test_plain_16384_parity(golden):
+@pytest.mark.parametrize("variant", [None, 163960])
+def test_plain_16384_parity(golden, variant):
+    """Fast mode, per-lane passes in reference arithmetic (default) and in
+    fast arithmetic (163960)."""
     g = golden("ref_c1_16384.npz")
     f64 = golden("fp64_c1_16384.npz")["rec100"]
-    out = run(C1, g["pos0"], [1, 100])
+    out = run(C1, g["pos0"], [1, 100], variant=variant)
     rec, nb = out[1]
     errs = field_errors(rec, g["rec1"])
     _report("16384 step 1", errs)
@@ -242,19 +245,25 @@ def test_kernel_variants_identical(golden, cell_mult):
 # lanes and 8 force lanes (264), relaxed force registers (268), packed
 # records (392), 4 and 16 force lanes (776, 1288), 16 density lanes (2312).
 COOP = (264, 268, 392, 776, 1288, 2312)
+# The fast-arithmetic variants (bit 131072: grouped products, fused
+# multiply-adds, r^2 for |r|^2, hardware 1/sqrt) of the list passes 88 and
+# 120|32768 and of the packed-record pass 216.
+FAST = (131160, 163960, 131288)
 
 
 @pytest.mark.parametrize("cell_mult", [1.0, 0.5])
 def test_cooperative_variants_within_tolerance(golden, cell_mult):
     """The cooperative passes sum each particle's terms in another order
-    (per-lane partial sums combined by a fixed shuffle tree), so they are
-    held to RTOL, not to the bits of the per-lane passes: every field within
-    RTOL of the reference after 1 step and of the per-lane passes after 30,
-    NeighbId equal after 1 step.  They are deterministic: graphs or eager
-    launches and either tile size give the same bits."""
+    (per-lane partial sums combined by a fixed shuffle tree), and the
+    fast-arithmetic passes round each term differently, so they are held to
+    RTOL, not to the bits of the per-lane passes: every field within RTOL of
+    the reference after 1 step and of the per-lane passes after 30, NeighbId
+    equal after 1 step (the in-range test is exact in every variant).  They
+    are deterministic: graphs or eager launches and either tile size give
+    the same bits."""
     g = golden("ref_c1_2048.npz")
     base = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=88)
-    for v in COOP:
+    for v in COOP + FAST:
         got = run(C1, g["pos0"], [1, 30], cell_mult=cell_mult, variant=v)
         e1 = field_errors(got[1][0], g["rec1"])
         e30 = field_errors(got[30][0], base[30][0])
@@ -263,9 +272,10 @@ def test_cooperative_variants_within_tolerance(golden, cell_mult):
         assert max(e1.values()) <= RTOL, v
         assert np.array_equal(got[1][1], g["nb1"]), v
         assert max(e30.values()) <= RTOL, v
-    a = run(C1, g["pos0"], 30, cell_mult=cell_mult, variant=264, graph_steps=16, tile=256)[30]
-    b = run(C1, g["pos0"], 30, cell_mult=cell_mult, variant=264, graph_steps=0, tile=128)[30]
-    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    for v in (264, 163960):
+        a = run(C1, g["pos0"], 30, cell_mult=cell_mult, variant=v, graph_steps=16, tile=256)[30]
+        b = run(C1, g["pos0"], 30, cell_mult=cell_mult, variant=v, graph_steps=0, tile=128)[30]
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), v
 
 
 def test_cooperative_overflow_path():

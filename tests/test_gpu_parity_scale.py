@@ -52,9 +52,10 @@ def _sample_check(O, op, st, base, delta, nb_prev, rec, nb, sed, ids, tag):
     assert ds.max() <= 1 + RTOL * max(1, np.abs(o["sed"]).max()), (tag, ds.max())
 
 
-@pytest.mark.parametrize("variant", [88, 264])
+@pytest.mark.parametrize("variant", [88, 264, 163960])
 def test_plain_1m_sampled_fields_vs_oracle(oracle_lib, variant):
-    """Per-lane passes (88) and cooperative passes (264)."""
+    """Per-lane passes (88), cooperative passes (264) and per-lane passes in
+    fast arithmetic with dynamically scheduled force warps (163960)."""
     import workloads as W
 
     O = oracle_lib
