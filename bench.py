@@ -564,19 +564,22 @@ def run_batched(args, config, embedded=False):
     sysm = S.System(particle_capacity=total + 512 * len(reqs), key_capacity=1 << 24, terrain_capacity=1 << 24,
                     tile=args.tile, graph_steps=16, device=local, variant=args.variant)
     scenes = [sysm.scene_from_request(base, r) for r in reqs]
-    # spin-up (untimed), then each scene's state is checkpointed so that the
-    # plain form starts every scene from the same state
+    # spin-up (untimed), the autotuner's pick (it restores the state it
+    # started from), then each scene's state is checkpointed so that the
+    # plain form starts every scene from the same state and runs the same
+    # warm-up and timed steps with the same kernels
     spin = spinup_steps(args, "batched")
     tmp = tempfile.mkdtemp(prefix="sph_bench_")
     if spin:
         sysm.step(spin)
+    sysm.sync()
+    tuned = sysm.autotune(4) if args.autotune else None
     paths = []
     for k, sc in enumerate(scenes):
         paths.append(os.path.join(tmp, f"scene{k}.sphe"))
         sc.save(paths[-1])
     sysm.step(args.warmup)
     sysm.sync()
-    tuned = sysm.autotune(4) if args.autotune else None
     if args.kernels_only:
         sysm.step(args.steps)
         sysm.sync()

@@ -131,17 +131,19 @@ def test_server_admission_respects_budget():
     assert before > 0
 
 
-def test_autotune_restores_state_and_applies_choice():
+def test_autotune_restores_state_and_applies_choice(tmp_path):
     """After tuning, the system continues from the untouched state with the
-    chosen tile and cell size: identical to a fresh run with that choice."""
+    chosen tile, cell size and kernel variant: identical to a run that takes
+    the same first steps, then continues in a fresh system with that choice
+    (some variants round differently, so the reference run uses the chosen
+    one too)."""
     reqs = SMALL[:3]
     with S.System(tile=256) as sysm:
         scenes = [sysm.scene_from_request(W.base_params(1.0), r) for r in reqs]
         sysm.step(5)
         before = [_state(sc) for sc in scenes]
         tuned = sysm.autotune(4)
-        assert len(tuned["tried"]) == 24 and tuned["tile"] in (128, 256)
-        assert tuned["variant"] in (0, 4, 28, 88, 120, 216)
+        assert len(tuned["tried"]) == 56 and tuned["tile"] in (128, 256)  # 2 tiles x 2 cell sizes x 14 variants
         assert tuned["ms_per_step"] == min(t[3] for t in tuned["tried"])
         for sc, st in zip(scenes, before):
             for a, b in zip(_state(sc), st):
@@ -149,16 +151,23 @@ def test_autotune_restores_state_and_applies_choice():
             assert sc.params().cell_mult == tuned["cell_mult"]
         sysm.step(10)
         after = [_state(sc) for sc in scenes]
-    # the same history without tuning: 5 steps, switch the cell size, 10 steps
-    # (the tile size never changes results)
+    # the same history without tuning: 5 steps, checkpoints, then 10 steps
+    # in a system with the chosen tile, cell size and variant
+    paths = []
     with S.System(tile=256) as ref:
         rs = [ref.scene_from_request(W.base_params(1.0), r) for r in reqs]
         ref.step(5)
-        for sc in rs:
+        for k, sc in enumerate(rs):
+            paths.append(str(tmp_path / f"s{k}.sphe"))
+            sc.save(paths[-1])
+    with S.System(tile=tuned["tile"], variant=tuned["variant"]) as ref2:
+        rs = [ref2.scene_from_request(W.base_params(tuned["cell_mult"]), r) for r in reqs]
+        for sc, path in zip(rs, paths):
+            sc.load(path)
             p = sc.params()
             p.cell_mult = tuned["cell_mult"]
             sc.set_params(p)
-        ref.step(10)
+        ref2.step(10)
         for sc, st in zip(rs, after):
             for a, b in zip(_state(sc), st):
                 assert np.array_equal(a, b)

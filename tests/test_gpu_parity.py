@@ -278,6 +278,19 @@ def test_cooperative_variants_within_tolerance(golden, cell_mult):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), v
 
 
+def test_fast_arithmetic_forms_identical(golden):
+    """The fast-arithmetic list passes in every launch form (packed records
+    or not, static or counter-scheduled warps) compute the same terms in the
+    same order: the same bits as one another."""
+    g = golden("ref_c1_2048.npz")
+    base = run(C1, g["pos0"], [1, 30], variant=131160)
+    for v in (131288, 163928, 163960, 164088):
+        got = run(C1, g["pos0"], [1, 30], variant=v)
+        for s in (1, 30):
+            assert np.array_equal(got[s][0], base[s][0]), (v, s)
+            assert np.array_equal(got[s][1], base[s][1]), (v, s)
+
+
 def test_cooperative_overflow_path():
     """Particles with more in-range neighbours than a list holds: the
     cooperative force pass splits their cell rows over the group instead;
