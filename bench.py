@@ -82,9 +82,9 @@ def source_digest() -> str:
 
 # The variant bits that select the force kernel (4 register budget, 8 lists,
 # 16 list walk loaded ahead, 128 packed records, 256 cooperative pass with
-# 512/1024 its group size, 32768 dynamically scheduled warp slices); the
-# others change only the density pass.
-FORCE_BITS = 4 | 8 | 16 | 128 | 256 | 512 | 1024 | 32768
+# 512/1024 its group size, 32768 dynamically scheduled warp slices, 131072
+# fast arithmetic); the others change only the density pass.
+FORCE_BITS = 4 | 8 | 16 | 128 | 256 | 512 | 1024 | 32768 | 131072
 
 
 def ncu_counters(workload, variant, cm):
@@ -117,7 +117,8 @@ def ingest_ncu(raw_csv, workload, variant, cm, command, kernel="k_force"):
     units = rows[1]
     col = {name: i for i, name in enumerate(head)}
     scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9,
-             "nsecond": 1e-9, "usecond": 1e-6, "msecond": 1e-3, "second": 1.0, "inst": 1.0, "": 1.0}
+             "nsecond": 1e-9, "usecond": 1e-6, "msecond": 1e-3, "second": 1.0, "ns": 1e-9, "us": 1e-6, "ms": 1e-3,
+             "s": 1.0, "inst": 1.0, "": 1.0}
 
     def val(r, name):
         i = col[name]
@@ -145,7 +146,8 @@ def ingest_ncu(raw_csv, workload, variant, cm, command, kernel="k_force"):
             data = json.load(f)
     except Exception:
         data = {"about": "ncu counters of the force kernel per launch (mean over the captured launches), "
-                         "read by bench.py for roofline.traffic and issue_roofline", "entries": []}
+                         "read by bench.py for roofline.traffic and issue_roofline; source_digest identifies the "
+                         "kernel sources captured, git_commit the checkout at ingestion", "entries": []}
     data["entries"] = [e for e in data["entries"]
                        if not (e["workload"] == workload and e["force_variant_bits"] == entry["force_variant_bits"]
                                and e["cell_mult"] == cm)] + [entry]
