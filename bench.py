@@ -446,6 +446,9 @@ def run_ours(args, spec, config):
     # the batched and served forms, in the same run
     extras = {}
     if args.extras and spec["name"] == "plain_1m":
+        # the served arm runs the kernels the plain scene's tuning picked (the
+        # server has no tuner of its own); the batched arm tunes itself
+        args.serve_variant = tuned["variant"] if tuned else args.variant
         base_cfg = {"h": W.H, "dt": W.PHYS["dt"], "erosion": True, "tile": args.tile, "cell_mult": args.cell_mult}
         extras["batched"] = run_batched(args, base_cfg, embedded=True)
         extras["serving"] = run_serving(args, base_cfg, embedded=True)
@@ -655,9 +658,10 @@ def run_serving(args, config, embedded=False):
     ws, rank, local = _init_ranks()
     full = W.serving_trace(args.requests, rate=args.rate)
     trace = shard.shard_requests(full, ws, rank)
+    variant = getattr(args, "serve_variant", None) or args.variant or 0
     with Clocks() as clk, S.Server(W.base_params(args.cell_mult), tile=args.tile, chunk_steps=16,
                                     hbm_budget=120 << 30, device=local, policy=1 if args.policy == "work" else 0,
-                                    max_active_particles=args.max_active) as srv:
+                                    max_active_particles=args.max_active, variant=variant) as srv:
         res, st = srv.run_trace(trace)
     lat = [r.done_s - r.arrival_s for r in res]
     bad = sum(1 for r in res if r.total_units != 0 or r.nan_particles != 0)
@@ -681,7 +685,8 @@ def run_serving(args, config, embedded=False):
            "data": "synthetic (seeded Poisson request trace)",
            "config": dict(config, workload="serving", requests=len(full), rate_per_s=args.rate,
                           hbm_budget_gb=120, parallelism=f"requests sharded over {ws} rank(s)",
-                          policy=args.policy, max_active_particles=args.max_active, trace_desc=desc),
+                          policy=args.policy, max_active_particles=args.max_active, variant=variant,
+                          trace_desc=desc),
            "p50_latency_s": pct(0.50), "p99_latency_s": pct(0.99), "max_latency_s": float(lat[-1]),
            "requests": int(len(lat)), "wall_s": wall, "peak_active": max(q["peak"] for q in parts),
            "peak_particles": max(q["peak_p"] for q in parts), "peak_bytes": max(q["peak_b"] for q in parts),

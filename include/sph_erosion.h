@@ -349,6 +349,11 @@ typedef struct sph_server_config {
     sph_params base;              /* physical constants of every scene */
     int policy;                   /* admission order among arrived requests: 0 = arrival,
                                      1 = least work (particles x steps) first */
+    int variant;                  /* kernel variant bits of the server's system (0 = the
+                                     library default, 88); with a variant that rounds
+                                     differently (fast arithmetic, cooperative passes) a
+                                     request's result is the same alone and in a mix while
+                                     the neighbour lists fit the budget */
 } sph_server_config;
 
 typedef struct sph_result {

@@ -147,6 +147,7 @@ class Server {
         s.graph_steps = c.chunk_steps > 0 ? c.chunk_steps : 16;
         s.hbm_budget = c.hbm_budget > 0 ? c.hbm_budget : ((int64_t)120 << 30);
         s.max_scenes = c.max_scenes > 0 ? c.max_scenes : 4096;
+        if (c.variant > 0) s.variant = c.variant;
         // arenas start small and grow within the budget as requests arrive
         s.particle_capacity = 1 << 16;
         s.key_capacity = 1 << 18;

@@ -95,7 +95,7 @@ class ServerStats(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("tile", C.c_int), ("cell_mult", C.c_float), ("chunk_steps", C.c_int),
                 ("hbm_budget", C.c_int64), ("max_active_particles", C.c_int64), ("max_scenes", C.c_int),
-                ("base", Params), ("policy", C.c_int)]
+                ("base", Params), ("policy", C.c_int), ("variant", C.c_int)]
 
 
 class TuneResult(C.Structure):
@@ -184,11 +184,12 @@ class Server:
     """Continuous-batching request server (include/sph_erosion.h)."""
 
     def __init__(self, base: Params = None, tile=256, cell_mult=0.5, chunk_steps=16, hbm_budget=0,
-                 max_active_particles=0, max_scenes=0, device=0, policy=0):
+                 max_active_particles=0, max_scenes=0, device=0, policy=0, variant=0):
         cfg = ServerConfig()
         lib().sph_server_config_default(C.byref(cfg))
         cfg.device, cfg.tile, cfg.cell_mult, cfg.chunk_steps = device, tile, cell_mult, chunk_steps
         cfg.policy = policy
+        cfg.variant = variant or 0
         if hbm_budget:
             cfg.hbm_budget = hbm_budget
         cfg.max_active_particles = max_active_particles

@@ -100,21 +100,27 @@ def test_step_budgets_retire_scenes_independently():
                 assert np.array_equal(a, b), r
 
 
-def test_server_results_same_alone_and_mixed():
+@pytest.mark.parametrize("variant", [0, 164088])
+def test_server_results_same_alone_and_mixed(variant):
+    """Each request's final state is the same served in a mix (overlapping
+    on the device) and served alone, with the library's default kernels and
+    with the fast-arithmetic ones the bench tunes to (lists fit the budget
+    in both runs)."""
     reqs = [dict(r, arrival_s=0.004 * i) for i, r in enumerate(SMALL)]
-    with S.Server(W.base_params(), chunk_steps=8) as srv:
+    with S.Server(W.base_params(), chunk_steps=8, variant=variant) as srv:
         mixed, stats = srv.run_trace(reqs)
     assert stats["completed"] == len(reqs)
     assert stats["peak_active"] >= 2  # requests really overlapped on the device
     for r, res in zip(reqs, mixed):
-        with S.Server(W.base_params(), chunk_steps=8) as one:
+        with S.Server(W.base_params(), chunk_steps=8, variant=variant) as one:
             (alone,), _ = one.run_trace([dict(r, arrival_s=0.0)])
         assert res.state_hash == alone.state_hash, r
         assert res.total_units == 0 and res.nan_particles == 0
         assert res.done_s >= res.admit_s >= res.arrival_s - 1e-6
-    # and the same state as stepping the scene directly through a system
-    _, dg = _alone(SMALL[1], SMALL[1]["steps"])
-    assert mixed[1].state_hash == dg["state_hash"] != 0
+    if variant == 0:
+        # and the same state as stepping the scene directly through a system
+        _, dg = _alone(SMALL[1], SMALL[1]["steps"])
+        assert mixed[1].state_hash == dg["state_hash"] != 0
     assert stats["p99_s"] >= stats["p50_s"] > 0
 
 
