@@ -211,3 +211,42 @@ def test_rainfall_100k_exact_mass_through_2000_steps():
     c0, c1 = columns(spec["pos"]), columns(st["pos"])
     print("column occupancy max/mean: start", c0.max() / c0.mean(), "after 2000 steps", c1.max() / c1.mean())
     assert c1.max() / c1.mean() > 1.2 * c0.max() / c0.mean()
+
+
+@pytest.mark.parametrize("variant", [88, 164088])
+def test_batched_scenes_sampled_fields_vs_oracle(oracle_lib, variant):
+    """The batched form against the oracle: eight of the seeded batched
+    scenes (4,532 to 47,055 particles, terrain sides 64 to 512) stepped
+    together in one system for 60 steps, then one more step of each checked
+    on 512 sampled particles against the oracle's FP32 step from that
+    scene's own state: every field within RTOL, NeighbId exact, sediment
+    within one unit.  Exact (88) and fast-arithmetic (164088) kernels."""
+    import workloads as W
+
+    O = oracle_lib
+    reqs = W.batched_requests(256)[:8]
+    base = S.default_params(**dict(W.PHYS, cell_mult=0.5, flags=S.SPH_FLAG_RECORD))
+    total = sum(r["particles"] for r in reqs)
+    with S.System(particle_capacity=total + 512 * len(reqs), key_capacity=1 << 22, terrain_capacity=1 << 20,
+                  variant=variant) as sysm:
+        scenes = [sysm.scene_from_request(base, r) for r in reqs]
+        bases = [sc.get_terrain()[0] for sc in scenes]  # before any erosion: the base heights
+        sysm.step(60)
+        states = []
+        for sc in scenes:
+            st = sc.get_particles()
+            _, dl = sc.get_terrain()
+            _, nb = sc.get_records()
+            states.append((st, dl, nb))
+        sysm.step(1)
+        for k, (sc, (st, dl, nb_prev), hb) in enumerate(zip(scenes, states, bases)):
+            n = sc.count()
+            rec, nb = sc.get_records()
+            after = sc.get_particles()
+            prm = S.params_dict(sc.params())
+            tw, td = sc.terrain_dims()
+            op = oracle_params(O, prm, terrain=(tw, td))
+            ids = np.sort(np.random.default_rng(k).choice(n, min(512, n), replace=False)).astype(np.int32)
+            _sample_check(O, op, st, hb, dl, nb_prev, rec, nb, after["sed"], ids,
+                          f"batched scene {k} ({n} particles, {tw}x{td}) variant {variant}")
+            assert sc.diag()["total_units"] == 0
