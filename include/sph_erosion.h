@@ -135,7 +135,11 @@ typedef struct sph_system_config {
                                      (grouped products, fused multiply-adds, r^2 for
                                      |r|^2, hardware 1/sqrt); exact in-range test, so the
                                      neighbour sets and NeighbId are unchanged, but not
-                                     the reference's rounding (within the 1e-4 bar);
+                                     the reference's rounding (within the 1e-4 bar),
+                            262144 = with 8 + 16 + 128 + 131072: the force pass gathers the
+                                     neighbours' packed records with TMA (tile::gather4) into
+                                     a shared-memory ring fed by a producer warp; same bits
+                                     as the other fast-arithmetic forms, slower (not tuned);
                                 default 88 (8 + 16 + 64) */
     int64_t hbm_budget;       /* bytes this system may hold (0 = unlimited) */
 } sph_system_config;

@@ -1067,6 +1067,51 @@ void System::ensure_nlist() {
         drop_graph();
     }
     nl_ready_ = true;
+    ensure_fmap();
+}
+
+// The tensor map of the packed records: fdat_ seen as a 2-D tensor of
+// float32, 8 wide (one particle's two float4), one row per arena particle,
+// copied one row per box (the shape tile::gather4 takes).  Built through the
+// driver's cuTensorMapEncodeTiled, reached via the runtime's entry-point
+// query; without it (or without packed records) the force pass keeps its
+// other forms.
+void System::ensure_fmap() {
+    if (!(cfg_.variant & 262144) || fdat_.n == 0) {
+        fmap_ok_ = false;
+        return;
+    }
+    const int64_t rows = fdat_.n / 2;
+    if (fmap_ok_ && fmap_base_ == fdat_.p && fmap_rows_ == rows) return;
+    fmap_ok_ = false;
+    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static Encode encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return;
+        }
+        encode = reinterpret_cast<Encode>(fn);
+    }
+    if (rows >= ((int64_t)1 << 31)) return;
+    const cuuint64_t dims[2] = {8, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {32};
+    const cuuint32_t box[2] = {8, 1};
+    const cuuint32_t elem[2] = {1, 1};
+    if (encode(&fmap_, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, fdat_.p, dims, strides, box, elem,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return;
+    fmap_base_ = fdat_.p;
+    fmap_rows_ = rows;
+    fmap_ok_ = true;
+    drop_graph();
 }
 
 DevArrays System::arrays() const {
@@ -1118,6 +1163,7 @@ LaunchShape System::shape() const {
     // after the counter ran out exit at once
     const int64_t slices = (int64_t)n_ptiles_ * (cfg_.tile / 32);
     s.grid_dyn = (int)std::min<int64_t>((slices * 32 + cfg_.tile - 1) / cfg_.tile, (int64_t)nsm_ * (2048 / cfg_.tile));
+    s.fmap = (nl_ready_ && fmap_ok_) ? &fmap_ : nullptr;
     return s;
 }
 
@@ -1225,6 +1271,7 @@ void System::check_status() {
     if (v & 1u)
         throw Error(SPH_ERR_DEVICE, "ordered mode: a particle had more in-range neighbours than the list holds");
     if (v & 2u) throw Error(SPH_ERR_DEVICE, "counting sort found inconsistent cell counts");
+    if (v & 4u) throw Error(SPH_ERR_DEVICE, "the force pass's TMA pipeline timed out waiting for a stage");
     throw Error(SPH_ERR_DEVICE, "kernel status " + std::to_string(v));
 }
 
@@ -1396,9 +1443,10 @@ void System::autotune(int steps, sph_tune_result* out) {
     // the force pass in dynamically scheduled warp slices; 163928, 163960,
     // 164088: the same in fast arithmetic, 164088 with packed records) and
     // cooperative passes (264: 32 + 8 lanes per particle, 776: 4 force
-    // lanes, 2312: 16 density lanes)
-    const int variants[] = {0,     4,      28,     88,     120, 216, 32856, 32888,
-                            163928, 163960, 164088, 264,    776, 2312};
+    // lanes, 2312: 16 density lanes).  The TMA gather pipeline (bit 18) is
+    // left out: 3-4x slower than 164088 on every state measured.
+    const int variants[] = {0,      4,      28,     88,  120, 216, 32856, 32888,
+                            163928, 163960, 164088, 264, 776, 2312};
     static_assert(2 * 2 * (sizeof variants / sizeof variants[0]) <= 64, "sph_tune_result holds 64 trials");
     float best = 1e30f;
     int bt = cfg_.tile, bv = cfg_.variant;

@@ -2,6 +2,7 @@
 // step orchestration and CUDA-graph capture.  Internal to libsph_gb300.so;
 // the public surface is include/sph_erosion.h.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -186,6 +187,13 @@ class System {
     DevBuf<int32_t> ncnt_;
     DevBuf<float4> fdat_;     // 2 per arena particle (variant bit 7)
     bool nl_ready_ = false;
+    // TMA map over fdat_ (one 32-byte row per particle) for the force
+    // pass's gather pipeline (variant bit 18); valid while fmap_ok_
+    CUtensorMap fmap_;
+    bool fmap_ok_ = false;
+    const float4* fmap_base_ = nullptr;
+    int64_t fmap_rows_ = 0;
+    void ensure_fmap();
     // key arena
     DevBuf<uint32_t> counts_, offsets_;
     DevBuf<uint32_t> chunk_;

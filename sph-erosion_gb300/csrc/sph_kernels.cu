@@ -17,6 +17,7 @@
 // intrinsic (__fmul_rn, __fadd_rn, ...), which the compiler never contracts
 // into a fused multiply-add, so each term rounds exactly like the reference's
 // scalar FP32 code.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -1306,6 +1307,183 @@ __global__ void __launch_bounds__(256, MINB) k_force_coop(DevArrays a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Force pass with a TMA gather pipeline (variant bit 18, with lists, packed
+// records and fast arithmetic).  Each block holds T consumer threads (one
+// particle of the tile each) and one producer warp.  For list slot q the
+// producer reads the T list entries (16-byte loads), keeps them in an index
+// ring in shared memory and issues TMA tile::gather4 copies of the T packed
+// records (rows of a 2-D tensor map over fdat, one row high) into a ring of
+// stages in shared memory; each stage's copies complete on its `full`
+// mbarrier, and the consumer warps release the stage through its `empty`
+// mbarrier.  The consumers then sum the same pairs in the same order as the
+// per-lane fast-arithmetic pass (the same bits), but their neighbour records
+// come from shared memory and hold no registers while in flight.  Every wait
+// is bounded by a clock limit; a wait that runs out sets status bit 2 and
+// ends the block's work.
+constexpr int kTmaRingBytes = 32768;  // record ring; stages = kTmaRingBytes / (T * 32)
+constexpr long long kWaitLimit = 4000000000LL;  // clock cycles (about 2 s)
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Waits until the phase of parity `parity` has completed; false when the
+// clock limit runs out first.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kWaitLimit) return false;
+    }
+}
+
+// Four rows (record indices) of the tensor map into 128 contiguous bytes of
+// shared memory; rows outside the tensor read as zeros.
+__device__ __forceinline__ void tma_gather4(void* dst, const CUtensorMap* map, int r0, int r1, int r2, int r3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+        "%3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kMaxTile + 32, MINB) k_force_tma(DevArrays a, const __grid_constant__ CUtensorMap fmap) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ int s_m;
+    const int T = (int)blockDim.x - 32;  // consumers: 128 or 256
+    const int D = kTmaRingBytes / (T * 32);
+    unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA wants 128-B rows
+    float4* ring = reinterpret_cast<float4*>(smem);  // stage s, lane l: ring[2 * (s * T + l) + {0, 1}]
+    uint32_t* jring = reinterpret_cast<uint32_t*>(smem + kTmaRingBytes);  // stage s, lane l: jring[s * T + l]
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTmaRingBytes + (size_t)D * T * 4);
+    uint64_t* empty = full + D;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const bool producer = tid >= T;
+    if (tid == 0) {
+        for (int q = 0; q < D; ++q) {
+            mbar_init(full + q, 1);
+            mbar_init(empty + q, (unsigned)(T / 32));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned it = 0;  // ring slots this block has used
+    bool ok = true;
+    const int nwork = *a.n_ptiles;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = a.ptiles[w];
+        if (a.steps_left[wk.scene] == 0) continue;
+        const SceneDev& S = a.scenes[wk.scene];
+        if (S.flags & kFlagOrdered) continue;
+        const int end = S.p_off + S.n;
+        if (producer) {
+            int m = 0;
+            for (int l = lane; l < T; l += 32) {
+                const int p = wk.start + l;
+                if (p < end) m = max(m, min(a.ncnt[p], kNbCap));
+            }
+            for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(kFull, m, o));
+            if (lane == 0) s_m = ok ? m : 0;
+        }
+        __syncthreads();
+        const int M = s_m;  // list slots in use in this tile
+        if (producer) {
+            const uint32_t* nl = a.nlist + (size_t)wk.start * kNbCap;
+            const int per = T / 32;  // consumer lanes per producer lane
+            for (int q = 0; q < M && ok; ++q) {
+                const unsigned i2 = it + (unsigned)q, st = i2 % (unsigned)D, ph = (i2 / (unsigned)D) & 1u;
+                if (i2 >= (unsigned)D && !mbar_wait(empty + st, ph ^ 1u)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t* e = nl + (size_t)q * T + per * lane;
+                uint4 jj[2];
+                for (int g = 0; g < per; g += 4) {
+                    jj[g / 4] = *reinterpret_cast<const uint4*>(e + g);
+                    *reinterpret_cast<uint4*>(jring + (size_t)st * T + per * lane + g) = jj[g / 4];
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive_expect_tx(full + st, (unsigned)(T * 32));
+                for (int g = 0; g < per; g += 4) {
+                    const uint4 v = jj[g / 4];
+                    tma_gather4(ring + 2 * ((size_t)st * T + per * lane + g), &fmap, S.p_off + (int)v.x,
+                                S.p_off + (int)v.y, S.p_off + (int)v.z, S.p_off + (int)v.w, full + st);
+                }
+            }
+        } else {
+            const int p0 = wk.start + tid;
+            const bool valid = p0 < end;
+            const int p = valid ? p0 : S.p_off;
+            const int pl = p - S.p_off;
+            const float4 xi = a.spos[p];
+            const float4 vi = a.svel[p];
+            const float4 di = a.dyn[p];
+            const float rho = di.x, Ai = di.y;
+            const int cnt = valid ? a.ncnt[p] : 0;
+            const bool listed = cnt <= kNbCap;
+            const bool rec = (S.flags & kFlagRecord) != 0;
+            const float4* sp = a.spos + S.p_off;
+            ForceAcc acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, -1, 0};
+            for (int q = 0; q < M; ++q) {
+                const unsigned i2 = it + (unsigned)q, st = i2 % (unsigned)D, ph = (i2 / (unsigned)D) & 1u;
+                if (ok && !mbar_wait(full + st, ph)) ok = false;
+                if (ok && listed && q < cnt) {
+                    const float4 r0 = ring[2 * ((size_t)st * T + tid)], r1 = ring[2 * ((size_t)st * T + tid) + 1];
+                    const uint32_t j = jring[(size_t)st * T + tid];
+                    const int idj = rec ? __float_as_int(__ldg(&sp[j].w)) : 0;
+                    const float rx = fs(xi.x, r0.x), ry = fs(xi.y, r0.y), rz = fs(xi.z, r0.z);
+                    force_pair_fast(S, acc, rx, ry, rz, dist2(rx, ry, rz), vi.x, vi.y, vi.z, Ai, r1, r0.w, r1.w, idj,
+                                    (int)j == pl);
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(empty + st);
+            }
+            if (valid && !listed) {
+                // the list overflowed: this lane walks its cells (same order)
+                const float4* sv = a.svel + S.p_off;
+                const float4* sd = a.dyn + S.p_off;
+                for_each_candidate(a, S, xi, [&](uint32_t j, float4 xj) {
+                    const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
+                    const float s2 = dist2(rx, ry, rz);
+                    if (s2 <= S.smax) {
+                        const float4 vj = __ldg(sv + j), dj = __ldg(sd + j);
+                        force_pair_fast(S, acc, rx, ry, rz, s2, vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z,
+                                        __float_as_int(xj.w), (int)j == pl);
+                    }
+                });
+            }
+            if (valid) integrate_and_store(a, S, p, xi, vi, rho, acc, true);
+        }
+        it += (unsigned)M;
+        __syncthreads();
+    }
+    if (!ok) atomicOr(a.status, 4u);
+}
+
+size_t force_tma_smem(int tile) {
+    const int D = kTmaRingBytes / (tile * 32);
+    return 128 + kTmaRingBytes + (size_t)D * tile * 4 + 2 * (size_t)D * 8;
+}
+
 // terrain: height snapshot = base + delta * unit, read by the next step.
 __global__ void __launch_bounds__(kMaxTile) k_terrain(DevArrays a) {
     const int nwork = *a.n_ttiles;
@@ -1643,6 +1821,11 @@ void launch_force(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
     // lane and need no shared memory; bit 15 (32768) has the pipelined list
     // walks take their work in warp slices from a counter (same bits)
     const bool dyn = (s.variant & 32768) != 0;
+    if ((s.variant & 262144) && (s.variant & (131072 | 128 | 24)) == (131072 | 128 | 24) && s.fmap) {
+        // bit 18: the TMA gather pipeline (fast arithmetic, packed records)
+        k_force_tma<3><<<s.grid_p, s.tile + 32, force_tma_smem(s.tile), st>>>(a, *static_cast<const CUtensorMap*>(s.fmap));
+        return;
+    }
     if ((s.variant & 131072) && (s.variant & 24) == 24) {
         // bit 17: fast arithmetic (force_pair_fast), pipelined list walk
         const bool pack = (s.variant & 128) != 0;

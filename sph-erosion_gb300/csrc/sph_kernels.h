@@ -51,7 +51,9 @@ struct DevArrays {
     // packed neighbour records (variant bit 7), two float4 per sorted
     // particle: (x, y, z, P/rho^2) and (vx, vy, vz, m/rho)
     float4* fdat;
-    // status word: bit 0 = ordered-mode neighbour overflow
+    // status word: bit 0 = ordered-mode neighbour overflow, bit 1 =
+    // inconsistent sort counts, bit 2 = a bounded wait of the TMA force
+    // pipeline ran out
     unsigned* status;
     // work counters of the dynamically scheduled neighbour kernels
     // ([0] density, [1] force), cleared by the reorder kernel every step;
@@ -70,6 +72,7 @@ struct LaunchShape {
     int grid_t;      // persistent grid of the terrain kernel
     int variant;     // sph_system_config.variant bits (bit 3 only with lists allocated)
     int grid_dyn;    // grid of the dynamically scheduled neighbour kernels
+    const void* fmap;  // host copy of the CUtensorMap over the packed records (null: none)
 };
 
 // Once per process and device: opt the list-traversal kernels into >48 KB of

@@ -191,6 +191,7 @@ extern "C" SPH_API int sph_density_static(const sph_params* p, int n, const floa
         s.grid_t = 0;
         s.variant = 0;
         s.grid_dyn = 0;
+        s.fmap = nullptr;
 
         const int nb = (n + 255) / 256;
         k_pack<<<nb, 256, 0, st>>>(pos3_dev, n, a.pos, a.vel);

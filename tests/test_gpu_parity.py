@@ -280,11 +280,12 @@ def test_cooperative_variants_within_tolerance(golden, cell_mult):
 
 def test_fast_arithmetic_forms_identical(golden):
     """The fast-arithmetic list passes in every launch form (packed records
-    or not, static or counter-scheduled warps) compute the same terms in the
-    same order: the same bits as one another."""
+    or not, static or counter-scheduled warps, the TMA gather pipeline)
+    compute the same terms in the same order: the same bits as one
+    another."""
     g = golden("ref_c1_2048.npz")
     base = run(C1, g["pos0"], [1, 30], variant=131160)
-    for v in (131288, 163928, 163960, 164088):
+    for v in (131288, 163928, 163960, 164088, 426232):
         got = run(C1, g["pos0"], [1, 30], variant=v)
         for s in (1, 30):
             assert np.array_equal(got[s][0], base[s][0]), (v, s)
