@@ -66,7 +66,7 @@ def port_calibration():
         return None
 
 
-COUNTERS = os.path.join(ROOT, "profiles", "counters_k_force.json")
+COUNTERS = os.path.join(ROOT, "profiles", "ncu_counters.json")
 KERNEL_SOURCES = ("sph_kernels.cu", "sph_kernels.h", "sph_types.h")
 
 
@@ -84,20 +84,26 @@ def source_digest() -> str:
 # 16 list walk loaded ahead, 128 packed records, 256 cooperative pass with
 # 512/1024 its group size, 32768 dynamically scheduled warp slices, 131072
 # fast arithmetic); the others change only the density pass.
-FORCE_BITS = 4 | 8 | 16 | 128 | 256 | 512 | 1024 | 32768 | 131072
+FORCE_BITS = 4 | 8 | 16 | 128 | 256 | 512 | 1024 | 32768 | 131072 | 262144
 
 
-def ncu_counters(workload, variant, cm):
-    """The force kernel's DRAM bytes and warp instructions per launch from
-    the committed ncu capture of the same workload, force kernel, cell size
-    and kernel sources; (None, reason) when no capture matches."""
+def variant_bits(kernel, variant):
+    """The bits of `variant` that select `kernel`'s code: FORCE_BITS for the
+    force pass, all of them for the density pass."""
+    return variant & FORCE_BITS if kernel == "k_force" else variant
+
+
+def ncu_counters(workload, variant, cm, kernel="k_force"):
+    """A neighbour kernel's DRAM bytes and warp instructions per launch from
+    the committed ncu capture of the same workload, kernel variant, cell
+    size and kernel sources; (None, reason) when no capture matches."""
     try:
         with open(COUNTERS) as f:
             entries = json.load(f)["entries"]
     except Exception:
         return None, "no ncu capture committed"
     dig = source_digest()
-    want = dict(workload=workload, force_variant_bits=variant & FORCE_BITS, cell_mult=cm)
+    want = dict(kernel=kernel, workload=workload, variant_bits=variant_bits(kernel, variant), cell_mult=cm)
     for e in entries:
         if all(e.get(k) == v for k, v in want.items()):
             if e.get("source_digest") != dig:
@@ -110,7 +116,7 @@ def ingest_ncu(raw_csv, workload, variant, cm, command, kernel="k_force"):
     """Reads `ncu -i <report> --page raw --csv` output, takes the launches of
     `kernel` (per launch: DRAM bytes read + written, warp instructions,
     duration) and records their mean as the counters of this workload,
-    force kernel, cell size and kernel sources in profiles/."""
+    kernel variant, cell size and kernel sources in profiles/."""
     with open(raw_csv, newline="") as f:
         rows = list(csv.reader(f))
     head = rows[0]
@@ -137,7 +143,7 @@ def ingest_ncu(raw_csv, workload, variant, cm, command, kernel="k_force"):
                                 text=True).stdout.strip() or None
     except Exception:
         commit = None
-    entry = dict(kernel=kernel, workload=workload, force_variant_bits=variant & FORCE_BITS, cell_mult=cm,
+    entry = dict(kernel=kernel, workload=workload, variant_bits=variant_bits(kernel, variant), cell_mult=cm,
                  variant=variant, source_digest=source_digest(), git_commit=commit, launches=len(launches),
                  dram_bytes_read=rd, dram_bytes_write=wr, dram_bytes=rd + wr, warp_instructions=inst,
                  ncu_duration_s=dur, command=command)
@@ -145,12 +151,12 @@ def ingest_ncu(raw_csv, workload, variant, cm, command, kernel="k_force"):
         with open(COUNTERS) as f:
             data = json.load(f)
     except Exception:
-        data = {"about": "ncu counters of the force kernel per launch (mean over the captured launches), "
-                         "read by bench.py for roofline.traffic and issue_roofline; source_digest identifies the "
-                         "kernel sources captured, git_commit the checkout at ingestion", "entries": []}
-    data["entries"] = [e for e in data["entries"]
-                       if not (e["workload"] == workload and e["force_variant_bits"] == entry["force_variant_bits"]
-                               and e["cell_mult"] == cm)] + [entry]
+        data = {"about": "ncu counters of the neighbour kernels per launch (mean over the captured launches), "
+                         "read by bench.py for roofline.traffic and issue_roofline; variant_bits are the variant "
+                         "bits that select the kernel's code, source_digest identifies the kernel sources "
+                         "captured, git_commit the checkout at ingestion", "entries": []}
+    key = ("kernel", "workload", "variant_bits", "cell_mult")
+    data["entries"] = [e for e in data["entries"] if any(e.get(k) != entry[k] for k in key)] + [entry]
     with open(COUNTERS, "w") as f:
         json.dump(data, f, indent=1)
         f.write("\n")
@@ -311,20 +317,24 @@ def traversal(scene, step_ms):
     """Neighbour-search counters at the end of the run: per particle, the
     candidates each of the two neighbour passes tests and the in-range pairs
     it evaluates; pair tests per second over the whole step; the spread of
-    in-range neighbour counts and the share of particles whose list (128
-    entries, self included) overflows, and of 32-particle warps holding one."""
+    in-range neighbour counts and the share of particles whose list
+    (the library's capacity, self included) overflows, and of
+    32-particle warps holding one."""
+    import sph_gb300 as S
+    cap = S.neighbour_list_capacity()
     t = scene.traversal_stats()
     n = max(t["particles"], 1)
     cnt = scene.neighbour_counts()  # by id; warps hold sorted order
     _, order = scene.debug_sort()
     c = cnt[order] + 1
-    over = c > 128
+    over = c > cap
     warps = over[: len(over) // 32 * 32].reshape(-1, 32).any(axis=1) if len(over) >= 32 else over
     return {"candidates_per_particle": t["candidates"] / n, "in_range_per_particle": t["in_range"] / n,
             "rows_per_particle": t["rows"] / n, "pair_tests_per_s": 2 * t["candidates"] / (step_ms * 1e-3),
             "in_range_pairs_per_s": 2 * t["in_range"] / (step_ms * 1e-3),
             "in_range_percentiles": {str(q): int(np.percentile(c, q)) for q in (50, 90, 99, 99.9, 100)},
-            "list_overflow_frac": float(over.mean()), "warps_with_overflow_frac": float(warps.mean()),
+            "list_capacity": cap, "list_overflow_frac": float(over.mean()),
+            "warps_with_overflow_frac": float(warps.mean()),
             "reference_pair_tests_per_step": 3 * n * n}
 
 
@@ -454,34 +464,39 @@ def run_ours(args, spec, config):
         extras["serving"] = run_serving(args, base_cfg, embedded=True)
     if rank != 0:
         return
-    # roofline of the dominant kernel (the force stage): algorithmic bytes =
-    # 48 B read (sorted pos, vel, density factors) + 32 B written (pos, vel)
-    # per particle + 4 B per terrain height read
+    # rooflines of the two neighbour kernels; the line's `roofline` is the
+    # one with the longer measured stage time.  Algorithmic bytes: density
+    # pass 16 B read (sorted position) + 16 B written (density factors) per
+    # particle; force pass 48 B read (sorted position, velocity, density
+    # factors) + 32 B written (position, velocity) per particle + 4 B per
+    # terrain height read
     hbm, kind = peaks()
     t = spec.get("terrain")
     texels = t["w"] * t["d"] if t else 0
-    force_ms = float(stages[5])
-    force_bytes = 80.0 * n + 4.0 * texels
-    achieved = force_bytes / (force_ms * 1e-3) / 1e9
     step_ms = tot / args.steps
     step_bytes = 88.0 * n + 16.0 * grid_cells + 20.0 * texels
     cpu_v, cores, m, _ = cpu_sample(spec, budget_s=args.ref_seconds)
     variant = tuned["variant"] if tuned else args.variant if args.variant is not None else 88
     cm = tuned["cell_mult"] if tuned else args.cell_mult
-    cnt, why = ncu_counters(config["workload"], variant, cm)
+    clk_sum = clk.summary()
+    roofs, issues = {}, {}
+    for kernel, ms, alg in (("k_density", float(stages[4]), 32.0 * n), ("k_force", float(stages[5]), 80.0 * n + 4.0 * texels)):
+        cnt, why = ncu_counters(config["workload"], variant, cm, kernel)
+        achieved = alg / (ms * 1e-3) / 1e9
+        roofs[kernel] = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": cnt["dram_bytes"] if cnt else None,
+                         "traffic_source": (f"ncu capture {cnt['source_digest']} ({cnt['command']})" if cnt else why),
+                         "algorithmic_bytes": alg, "peak_kind": kind, "stage_ms": ms}
+        issues[kernel] = issue_roofline(cnt, ms, clk_sum, kernel)
+    dominant = max(roofs, key=lambda k: roofs[k]["stage_ms"])
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + fBm terrain)",
         "config": config,
-        "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm,
-                     "traffic": cnt["dram_bytes"] if cnt else None,
-                     "traffic_source": (f"ncu capture {cnt['source_digest']} ({cnt['command']})" if cnt else why),
-                     "algorithmic_bytes": force_bytes,
-                     "peak_kind": kind,
-                     "step_bytes_frac": step_bytes / (step_ms * 1e-3) / 1e9 / hbm},
-        "issue_roofline": issue_roofline(cnt, force_ms, clk.summary()),
+        "roofline": dict(roofs[dominant], step_bytes_frac=step_bytes / (step_ms * 1e-3) / 1e9 / hbm),
+        "issue_roofline": issues[dominant],
+        "rooflines": {k: {"hbm": roofs[k], "issue": issues[k]} for k in roofs},
         "cpu_baseline": dict({"value": cpu_v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                               "sample": f"{m} of {n} particles x 3 all-pairs passes + integration per step"},
                              **calibration_keys()),
@@ -491,7 +506,7 @@ def run_ours(args, spec, config):
                      "d2h_bytes_per_step": int(n * 12), "readback": "blocking into pageable memory"},
         "gpu_launches": int(args.steps * (7 if t else 6)),
         "stages_ms": {name: float(v) for name, v in zip(S.STAGES, stages)},
-        "clocks": clk.summary(),
+        "clocks": clk_sum,
         "device_bytes": dev_bytes,
         "mass_units_total": int(d["total_units"]),
         "diag_fp64": {"kinetic": d["kinetic"], "potential": d["potential"], "momentum": d["momentum"],
@@ -511,21 +526,21 @@ def run_ours(args, spec, config):
 C_PARAMS_BYTES = 248 + 4
 
 
-def issue_roofline(cnt, force_ms, clocks):
-    """The force kernel against the instruction-issue peak: warp
-    instructions per launch (the ncu capture of the same workload, force
-    kernel, cell size and sources) over the live CUDA-event time, against 4
+def issue_roofline(cnt, ms, clocks, kernel):
+    """A neighbour kernel against the instruction-issue peak: warp
+    instructions per launch (the ncu capture of the same workload, kernel
+    variant, cell size and sources) over the live CUDA-event time, against 4
     per cycle per SM at the sampled SM clock."""
     inst = cnt["warp_instructions"] if cnt else None
-    if inst is None or not force_ms:
+    if inst is None or not ms:
         return None
     import torch
 
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
     peak = 4.0 * sms * mhz * 1e6
-    achieved = inst / (force_ms * 1e-3)
-    return {"kernel": "k_force", "achieved": achieved, "peak": peak, "unit": "warp-instructions/s",
+    achieved = inst / (ms * 1e-3)
+    return {"kernel": kernel, "achieved": achieved, "peak": peak, "unit": "warp-instructions/s",
             "frac": achieved / peak, "warp_instructions_per_launch": inst, "source": "ncu smsp__inst_executed.sum"}
 
 
@@ -764,13 +779,15 @@ def main():
     ap.add_argument("--dry-run", action="store_true",
                     help="rank plumbing only, without CUDA: each rank joins the barrier, rank 0 prints n_gpus")
     ap.add_argument("--ingest-ncu", default=None, metavar="RAW_CSV",
-                    help="record the force kernel's counters from `ncu -i REPORT --page raw --csv` output for "
-                         "--workload/--variant/--cell-mult into profiles/counters_k_force.json")
+                    help="record a neighbour kernel's counters from `ncu -i REPORT --page raw --csv` output for "
+                         "--workload/--variant/--cell-mult into profiles/ncu_counters.json")
     ap.add_argument("--ingest-command", default="", help="with --ingest-ncu: the capture command, as run")
+    ap.add_argument("--ingest-kernel", default="k_force", choices=("k_force", "k_density"),
+                    help="with --ingest-ncu: the kernel whose launches to record")
     args = ap.parse_args()
     if args.ingest_ncu:
         ingest_ncu(args.ingest_ncu, args.workload, args.variant if args.variant is not None else 88, args.cell_mult,
-                   args.ingest_command)
+                   args.ingest_command, args.ingest_kernel)
         return
     if "WORLD_SIZE" not in os.environ and args.gpus > 1:
         sys.exit(launch_ranks(args.gpus))

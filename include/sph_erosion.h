@@ -115,7 +115,7 @@ typedef struct sph_system_config {
                                  1 = density pass over compacted neighbour lists,
                                  4 = relaxed register budget (fewer resident blocks),
                                  8 = the density pass writes each particle's in-range
-                                     neighbours (128 slots, 516 B per particle) and the
+                                     neighbours (192 slots, 772 B per particle) and the
                                      force pass reads them instead of re-testing the
                                      cells; ignored when the HBM budget has no room,
                                 16 = with 8: the force pass's list walk loads ahead,
@@ -313,6 +313,9 @@ SPH_API int sph_scene_debug_sort(sph_system* s, int scene, uint32_t* keys_by_id,
 /* In-range neighbour count (|x_i - x_j| <= h, j != i; fluid_system.h:139-142)
  * of each particle, in id order, from the uniform-grid traversal. */
 SPH_API int sph_scene_neighbour_counts(sph_system* s, int scene, int32_t* counts_by_id);
+/* Entries a neighbour list holds (self included); a particle with more
+ * in-range neighbours walks the cells in the force pass instead. */
+SPH_API int sph_neighbour_list_capacity(void);
 /* Grid dims used by the sort: nx ny nz nkeys. */
 SPH_API int sph_scene_grid_dims(sph_system* s, int scene, int* dims4);
 /* Counters of the neighbour search the next step would run, from the current

@@ -333,6 +333,8 @@ int sph_scene_neighbour_counts(sph_system* s, int scene, int32_t* counts_by_id) 
     });
 }
 
+int sph_neighbour_list_capacity(void) { return sph::kNbCap; }
+
 int sph_scene_grid_dims(sph_system* s, int scene, int* dims4) {
     return guard([&] {
         need(dims4, "dims");

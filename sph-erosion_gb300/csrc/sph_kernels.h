@@ -63,7 +63,7 @@ struct DevArrays {
 };
 
 // Slots per particle of the in-range neighbour lists.
-constexpr int kNbCap = 128;
+constexpr int kNbCap = 192;
 
 struct LaunchShape {
     int tile;        // threads per particle tile

@@ -148,6 +148,7 @@ SIGNATURES = {
     "sph_scene_terrain_dims": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sph_scene_debug_sort": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "sph_scene_neighbour_counts": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "sph_neighbour_list_capacity": (C.c_int, []),
     "sph_scene_grid_dims": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "sph_density_static": (C.c_int, [C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sph_scene_from_request": (C.c_int, [C.c_void_p, C.POINTER(Params), C.POINTER(Request), C.POINTER(C.c_int)]),
@@ -293,6 +294,11 @@ def grid_collision(hmap, dims, cur, nxt, vel):
     _ck(lib().sph_grid_collision_u8(_p(m), int(dx), int(dz), n, _p(cur), _p(nxt), _p(vel), _p(cp), _p(nr),
                                     _p(hit)))
     return hit.astype(bool), cp, nr
+
+
+def neighbour_list_capacity() -> int:
+    """Entries one particle's neighbour list holds, self included."""
+    return lib().sph_neighbour_list_capacity()
 
 
 def default_params(**overrides) -> Params:

@@ -47,3 +47,39 @@ def test_gpus_flag_launches_ranks_dry_run():
         assert len(lines) == 1, r.stdout
         assert lines[0]["n_gpus"] == 2 and lines[0]["dry_run"] and lines[0]["impl"] == impl
         assert lines[0]["max_over_ranks_s"] == 0.002  # rank 1's value: the max over ranks
+
+
+def test_ncu_counters_ingest_and_match(tmp_path, monkeypatch):
+    """Counters ingested from an ncu raw CSV are found again only for the
+    same kernel, workload, kernel variant bits, cell size and kernel
+    sources: the force pass ignores the density-only bits, the density pass
+    does not."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    monkeypatch.setattr(bench, "COUNTERS", str(tmp_path / "counters.json"))
+    raw = tmp_path / "raw.csv"
+    names = ["Kernel Name", "dram__bytes_read.sum", "dram__bytes_write.sum", "smsp__inst_executed.sum",
+             "gpu__time_duration.sum"]
+    rows = [names, ["", "Mbyte", "Kbyte", "inst", "usecond"],
+            ["void k_force<0, 4, 3, 1, 1>(DevArrays)", "400.5", "2,000", "1000", "500"],
+            ["void k_force<0, 4, 3, 1, 1>(DevArrays)", "399.5", "1,000", "3000", "700"],
+            ["void k_density<0, 0, 4, 1, 1, 1, 0, 1>(DevArrays)", "100", "10", "10", "400"]]
+    raw.write_text("\n".join(",".join(f'"{c}"' for c in r) for r in rows) + "\n")
+    v = 164088
+    bench.ingest_ncu(str(raw), "plain_1m", v, 0.5, "cmd-f", "k_force")
+    bench.ingest_ncu(str(raw), "plain_1m", v, 0.5, "cmd-d", "k_density")
+    f, why = bench.ncu_counters("plain_1m", v, 0.5, "k_force")
+    assert why is None and f["launches"] == 2 and f["command"] == "cmd-f"
+    assert abs(f["dram_bytes"] - (400e6 + 1.5e6)) < 1 and f["warp_instructions"] == 2000
+    assert abs(f["ncu_duration_s"] - 600e-6) < 1e-12
+    d, why = bench.ncu_counters("plain_1m", v, 0.5, "k_density")
+    assert why is None and d["launches"] == 1 and abs(d["dram_bytes"] - (100e6 + 10e3)) < 1
+    # bit 64 selects density code only: the force entry still matches
+    assert bench.ncu_counters("plain_1m", v & ~64, 0.5, "k_force")[0] is not None
+    assert bench.ncu_counters("plain_1m", v & ~64, 0.5, "k_density")[0] is None
+    assert bench.ncu_counters("plain_1m", v, 1.0, "k_force")[0] is None
+    # counters of other kernel sources are not reported as this build's
+    monkeypatch.setattr(bench, "source_digest", lambda: "0" * 16)
+    e, why = bench.ncu_counters("plain_1m", v, 0.5, "k_force")
+    assert e is None and "other kernel sources" in why

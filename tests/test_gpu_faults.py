@@ -135,8 +135,8 @@ def test_server_runs_a_request_without_lists_when_only_they_do_not_fit():
     with S.Server(W.base_params(), chunk_steps=8) as roomy:
         (ra_lists,), st = roomy.run_trace([dict(a, arrival_s=0.0)])
     # the server samples its memory when it admits, before the first step
-    # allocates the lists; those are 516 B per particle of the particle
-    # arena (at least 2^16 particles: 33.8 MB), so 16 MB more than that peak
+    # allocates the lists; those are 772 B per particle of the particle
+    # arena (at least 2^16 particles: 50.6 MB), so 16 MB more than that peak
     # holds everything but them
     budget = int(st["peak_bytes"]) + (16 << 20)
     with S.Server(W.base_params(), chunk_steps=8, hbm_budget=budget) as srv:

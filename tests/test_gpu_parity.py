@@ -308,7 +308,7 @@ def test_cooperative_overflow_path():
 
 
 def test_neighbour_list_overflow_falls_back_exactly():
-    """Particles with more in-range neighbours than a list holds (64) make
+    """Particles with more in-range neighbours than a list holds (192) make
     their warp traverse the cells again: same bits as without lists."""
     rng = np.random.default_rng(5)
     blob = rng.uniform(-0.006, 0.006, (300, 3))
@@ -322,7 +322,7 @@ def test_neighbour_list_overflow_falls_back_exactly():
 
 
 def test_ordered_mode_neighbour_overflow_is_reported():
-    """More than 128 in-range neighbours in ordered mode must not pass
+    """More than 128 in-range neighbours (the ordered traversal's sort buffer) in ordered mode must not pass
     unnoticed: the kernel sets a status bit and the next read raises."""
     rng = np.random.default_rng(3)
     pos = (rng.uniform(-0.005, 0.005, (300, 3))).astype(np.float32)
