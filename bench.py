@@ -614,6 +614,8 @@ def run_batched(args, config, embedded=False):
     d1 = sysm.diag_many(scenes)
     batched = total_all * args.steps / (ms * 1e-3)
     bad = sum(1 for d in d1 if d["total_units"] != 0 or d["nan_particles"] != 0)
+    # per-stage CUDA-event times of a few more steps (after the fingerprints)
+    stages = sysm.profile_stages(max(3, min(args.steps, 10)))
     sysm.close()
     # plain form: one system per scene, same steps, same tuned tile and cell
     tile = tuned["tile"] if tuned else args.tile
@@ -651,11 +653,12 @@ def run_batched(args, config, embedded=False):
                           l2="inputs larger than L2 (%.0f MB of particle state)" % (total_all * 100 / 1e6)),
            "plain_value": plain, "batched_over_plain": batched / plain, "plain_ms_per_step": plain_ms / args.steps,
            "alone_equals_batched": f"{same} of {len(all_reqs)} scenes (state fingerprint after the timed steps)",
-           "mass_violations": bad, "tuned": tuned, "clocks": clk.summary()}
+           "mass_violations": bad, "tuned": tuned, "clocks": clk.summary(),
+           "stages_ms": {name: float(v) for name, v in zip(S.STAGES, stages)}}
     if embedded:
         return {k: res[k] for k in ("value", "unit", "ms_per_step", "plain_value", "plain_ms_per_step",
                                     "batched_over_plain", "alone_equals_batched", "mass_violations", "tuned",
-                                    "clocks", "config")}
+                                    "clocks", "config", "stages_ms")}
     print(json.dumps(res), flush=True)
     return None
 

@@ -38,7 +38,7 @@ class OracleParams(C.Structure):
 
 class OracleGrid(C.Structure):
     _fields_ = [
-        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("by", C.c_int), ("bz", C.c_int),
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
         ("nkeys", C.c_int), ("cell", C.c_float), ("inv_cell", C.c_float), ("lo", C.c_float * 3),
     ]
 

@@ -206,12 +206,7 @@ void oracle_neighbour_counts(int n, const float* pos, float h, int* counts, int 
     }
 }
 
-/* ---- uniform grid: Morton-row keys and stable counting sort --------------- */
-static int bits_for(int n) {
-    int b = 0;
-    while ((1 << b) < n) b++;
-    return b;
-}
+/* ---- uniform grid: row keys and stable counting sort ---------------------- */
 
 /* Cell edge = h * cell_mult * (1 + 2^-12): the small slack guarantees that two
  * particles within h never land more than ceil(1/cell_mult) cells apart after
@@ -231,9 +226,7 @@ void oracle_grid_make(const oracle_params* p, float cell_mult, oracle_grid* g) {
     g->nx = dims[0];
     g->ny = dims[1];
     g->nz = dims[2];
-    g->by = bits_for(g->ny);
-    g->bz = bits_for(g->nz);
-    g->nkeys = (g->nx << (g->by + g->bz)) + 1;
+    g->nkeys = g->nx * g->ny * g->nz + 1;
 }
 
 static int cell_coord(float x, float lo, float inv, int n) {
@@ -243,24 +236,14 @@ static int cell_coord(float x, float lo, float inv, int n) {
     return (int)t;
 }
 
-/* (y, z) interleave: bit b of y, then bit b of z, for b = 0, 1, ... while
- * each coordinate still has bits; the row index is then scaled by nx. */
-static uint32_t yz_morton(int cy, int cz, int by, int bz) {
-    uint32_t m = 0;
-    int b, o = 0;
-    int top = by > bz ? by : bz;
-    for (b = 0; b < top; b++) {
-        if (b < by) m |= (uint32_t)((cy >> b) & 1) << o++;
-        if (b < bz) m |= (uint32_t)((cz >> b) & 1) << o++;
-    }
-    return m;
-}
+/* row index of cell row (y, z), y fastest; the key is row * nx + x */
+static uint32_t yz_row(int cy, int cz, int ny) { return (uint32_t)cy + (uint32_t)cz * (uint32_t)ny; }
 
 uint32_t oracle_cell_key(const oracle_grid* g, float x, float y, float z) {
     int cx = cell_coord(x, g->lo[0], g->inv_cell, g->nx);
     int cy = cell_coord(y, g->lo[1], g->inv_cell, g->ny);
     int cz = cell_coord(z, g->lo[2], g->inv_cell, g->nz);
-    return yz_morton(cy, cz, g->by, g->bz) * (uint32_t)g->nx + (uint32_t)cx;
+    return yz_row(cy, cz, g->ny) * (uint32_t)g->nx + (uint32_t)cx;
 }
 
 void oracle_cell_keys(const oracle_grid* g, int n, const float* pos, uint32_t* keys) {

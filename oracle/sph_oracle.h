@@ -97,11 +97,10 @@ double oracle_time_sample(const oracle_params* p, int n, const float* pos, const
 /* Neighbour counts with the reference's test |x_i - x_j| <= h, j != i. */
 void oracle_neighbour_counts(int n, const float* pos, float h, int* counts, int nthreads);
 
-/* Uniform-grid restatement: cell dims, Morton-row keys and stable order. */
+/* Uniform-grid restatement: cell dims, row keys and stable order. */
 typedef struct oracle_grid {
     int nx, ny, nz;
-    int by, bz;        /* bits of the y and z Morton interleave */
-    int nkeys;         /* nx << (by+bz), plus one sentinel key */
+    int nkeys;         /* nx * ny * nz, plus one sentinel key */
     float cell;        /* cell edge */
     float inv_cell;
     float lo[3];       /* grid origin (box minimum) */

@@ -23,13 +23,6 @@ constexpr int64_t kMaxArenaIndex = ((int64_t)1 << 31) - ((int64_t)1 << 20);
 
 int64_t round_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
-int bits_for(int n) {
-    int b = 0;
-    while ((1 << b) < n) ++b;
-    return b;
-}
-
-
 inline float bits_to_float(int v) {
     float f;
     std::memcpy(&f, &v, sizeof f);
@@ -43,18 +36,9 @@ inline int float_to_bits(float f) {
 
 }  // namespace
 
-// (y, z) Morton interleave of the row index: bit b of y, then bit b of z,
-// while each coordinate still has bits.
-uint32_t yz_interleave(int cy, int cz, int by, int bz) {
-    uint32_t m = 0;
-    int o = 0;
-    const int top = std::max(by, bz);
-    for (int b = 0; b < top; ++b) {
-        if (b < by) m |= (uint32_t)((cy >> b) & 1) << o++;
-        if (b < bz) m |= (uint32_t)((cz >> b) & 1) << o++;
-    }
-    return m;
-}
+// Row index of cell row (y, z): y + z * ny (rows of one z-slab adjacent,
+// no padding of the key space).
+uint32_t yz_row(int cy, int cz, int ny) { return (uint32_t)cy + (uint32_t)cz * (uint32_t)ny; }
 
 // Largest float s with sqrtf(s) <= h.  sqrtf is correctly rounded and
 // monotonic, so for every float s >= 0: sqrtf(s) <= h  <=>  s <= smax.  The
@@ -423,9 +407,7 @@ void System::geometry(Scene& sc) {
     sc.nx = d[0];
     sc.ny = d[1];
     sc.nz = d[2];
-    sc.by = bits_for(sc.ny);
-    sc.bz = bits_for(sc.nz);
-    const int64_t nk = ((int64_t)sc.nx << (sc.by + sc.bz)) + 1;
+    const int64_t nk = (int64_t)sc.nx * sc.ny * sc.nz + 1;
     if (nk > (int64_t)1 << 30) throw Error(SPH_ERR_CAPACITY, "uniform grid too large (raise cell_mult or shrink the box)");
     sc.nkeys = (int)nk;
     sc.k_cap = (int)round_up(nk, kChunk);
@@ -594,10 +576,10 @@ int System::create_scene(const sph_params& p, int capacity, int tw, int td) {
         rec_.resize(pos_.n * kRecFloats, false, st_);
         drop_graph();
     }
-    // interleave tables and clean key ranges
+    // row tables and clean key ranges
     std::vector<uint32_t> tab(sc.tab_len);
-    for (int y = 0; y < sc.ny; ++y) tab[y] = yz_interleave(y, 0, sc.by, sc.bz);
-    for (int z = 0; z < sc.nz; ++z) tab[sc.ny + z] = yz_interleave(0, z, sc.by, sc.bz);
+    for (int y = 0; y < sc.ny; ++y) tab[y] = yz_row(y, 0, sc.ny);
+    for (int z = 0; z < sc.nz; ++z) tab[sc.ny + z] = yz_row(0, z, sc.ny);
     SPH_CK(cudaMemcpyAsync(tab_.p + sc.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
     SPH_CK(cudaMemsetAsync(counts_.p + sc.k_off, 0, (size_t)sc.k_cap * 4, st_));
     SPH_CK(cudaMemsetAsync(chunk_.p + sc.c_off, 0, (size_t)sc.nchunks * 4, st_));
@@ -663,8 +645,8 @@ void System::set_params(int id, const sph_params& p) {
             g.c_off = co;
             g.tab_off = to;
             std::vector<uint32_t> tab(g.tab_len);
-            for (int y = 0; y < g.ny; ++y) tab[y] = yz_interleave(y, 0, g.by, g.bz);
-            for (int z = 0; z < g.nz; ++z) tab[g.ny + z] = yz_interleave(0, z, g.by, g.bz);
+            for (int y = 0; y < g.ny; ++y) tab[y] = yz_row(y, 0, g.ny);
+            for (int z = 0; z < g.nz; ++z) tab[g.ny + z] = yz_row(0, z, g.ny);
             SPH_CK(cudaMemcpyAsync(tab_.p + g.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
             SPH_CK(cudaMemsetAsync(counts_.p + g.k_off, 0, (size_t)g.k_cap * 4, st_));
             SPH_CK(cudaMemsetAsync(chunk_.p + g.c_off, 0, (size_t)g.nchunks * 4, st_));
@@ -680,8 +662,8 @@ void System::set_params(int id, const sph_params& p) {
         }
     } else if (ng.nx != sc.nx || ng.ny != sc.ny || ng.nz != sc.nz) {
         std::vector<uint32_t> tab(ng.tab_len);
-        for (int y = 0; y < ng.ny; ++y) tab[y] = yz_interleave(y, 0, ng.by, ng.bz);
-        for (int z = 0; z < ng.nz; ++z) tab[ng.ny + z] = yz_interleave(0, z, ng.by, ng.bz);
+        for (int y = 0; y < ng.ny; ++y) tab[y] = yz_row(y, 0, ng.ny);
+        for (int z = 0; z < ng.nz; ++z) tab[ng.ny + z] = yz_row(0, z, ng.ny);
         SPH_CK(cudaMemcpyAsync(tab_.p + ng.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
     }
     if ((p.flags & SPH_FLAG_RECORD) && rec_.n == 0) {

@@ -68,7 +68,7 @@ struct Scene {
     int n = 0;
     int p_cap = 0;
     int64_t p_off = 0;
-    int nx = 1, ny = 1, nz = 1, by = 0, bz = 0, reach = 1;
+    int nx = 1, ny = 1, nz = 1, reach = 1;
     int nkeys = 0, k_cap = 0, nchunks = 0;
     int64_t k_off = 0, c_off = 0, tab_off = 0;
     int tab_len = 0;
@@ -230,8 +230,8 @@ void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, floa
 
 // Sets the calling thread's sph_last_error() message (sph_capi.cu).
 void set_last_error(const std::string& msg);
-// Interleave-table entry of a grid row: the (y, z) Morton index.
-uint32_t yz_interleave(int cy, int cz, int by, int bz);
+// Row-table entry of cell row (y, z): y + z * ny.
+uint32_t yz_row(int cy, int cz, int ny);
 
 // Terrain meshes (sph_mesh.cu).
 void mesh_u8(const unsigned char* map_host, int dimx, int dimy, int dimz, float* verts, unsigned* idx,
