@@ -55,6 +55,18 @@ def ulp_diff(a, b):
     return np.abs(a - b)
 
 
+def height_unit(prm: dict, terrain):
+    """The product's terrain height per delta unit, FP32: (mass / rest_density)
+    * 2^-30 over the area of one vertex cell of a (w, d) terrain."""
+    tw, td = terrain
+    bh = prm.get("box_half", (0.2, 0.2, 0.2))
+    f32 = np.float32
+    sx = f32(f32(f32(bh[0]) + f32(bh[0])) / f32(tw - 1))
+    sz = f32(f32(f32(bh[2]) + f32(bh[2])) / f32(td - 1))
+    return f32((float(f32(prm.get("mass", 0.02))) / float(f32(prm.get("rest_density", 998.29)))) * 2.0 ** -30
+               / (float(sx) * float(sz)))
+
+
 def oracle_params(O, prm: dict, terrain=None):
     """The oracle's parameter block for a product parameter dict (same FP32
     values); with terrain=(w, d) the height unit follows the product's rule:
@@ -66,10 +78,7 @@ def oracle_params(O, prm: dict, terrain=None):
               box_c=prm.get("box_center", (0.0, 0.0, 0.0)), box_l=bh)
     if terrain is not None:
         tw, td = terrain
-        f32 = np.float32
-        sx = f32(f32(f32(bh[0]) + f32(bh[0])) / f32(tw - 1))
-        sz = f32(f32(f32(bh[2]) + f32(bh[2])) / f32(td - 1))
-        hu = f32((float(f32(kw["mass"])) / float(f32(kw["p0"]))) * 2.0 ** -30 / (float(sx) * float(sz)))
+        hu = height_unit(prm, terrain)
         kw.update(terrain=(tw, td), height_unit=float(hu), erosion=bool(prm.get("erosion", 0)),
                   k_capacity=prm.get("k_capacity", 0.01), k_pickup=prm.get("k_pickup", 5.0),
                   k_deposit=prm.get("k_deposit", 2.0), layer=prm.get("erosion_layer", 0.0457))

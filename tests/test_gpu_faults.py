@@ -57,16 +57,17 @@ def test_refused_grid_resize_keeps_the_scene_running():
     """A parameter change whose finer grid does not fit the budget is refused
     and the scene continues with its old parameters, bit for bit."""
     req = dict(seed=11, particles=2000, terrain_side=64, steps=0)
-    with S.System() as probe:
+    cfg = dict(key_capacity=4096)  # key arena sized by the scene, so a finer grid must grow it
+    with S.System(**cfg) as probe:
         sc = probe.scene_from_request(W.base_params(), req)
         need = probe.memory()
         probe.step(5)
         want = sc.get_particles()["pos"]
-    with S.System(hbm_budget=need + (512 << 10)) as sysm:
+    with S.System(hbm_budget=need + (256 << 10), **cfg) as sysm:
         sc = sysm.scene_from_request(W.base_params(), req)
         p = sc.params()
         old = p.cell_mult
-        p.cell_mult = 0.25
+        p.cell_mult = 0.25  # 8 times the cells: at least 400 KB more keys than the 256 KB of slack
         with pytest.raises(S.SphError) as e:
             sc.set_params(p)
         assert e.value.code == -4

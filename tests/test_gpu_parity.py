@@ -25,7 +25,7 @@ import numpy as np
 import pytest
 
 import sph_gb300 as S
-from helpers import C1, REF, RTOL, field_errors, oracle_params, run, run_terrain, ulp_diff
+from helpers import C1, REF, RTOL, field_errors, height_unit, oracle_params, run, run_terrain, ulp_diff
 
 pytestmark = pytest.mark.gpu
 
@@ -375,6 +375,9 @@ def test_terrain_erosion_parity_and_exact_mass(oracle_lib, ordered):
         x = O.run(op, pos, vel, nsteps=s, base=heights, precision="f32x")
         # exact mass: sediment + terrain units are conserved to the last unit
         assert dg["total_units"] == 0 and int(sed.astype(np.int64).sum()) + int(dl.sum()) == 0
+        # the height snapshot is base + delta * unit at every vertex
+        hu = height_unit(prm, heights.shape[::-1])
+        assert np.array_equal(hg, heights.astype(np.float32) + dl.astype(np.float32) * hu), s
         assert dg["sediment_units"] == int(sed.astype(np.int64).sum())
         if ordered:
             assert np.array_equal(rec, x["rec"]), s
@@ -383,6 +386,25 @@ def test_terrain_erosion_parity_and_exact_mass(oracle_lib, ordered):
             assert max(field_errors(rec, x["rec"]).values()) <= RTOL
             assert np.abs(sed.astype(np.int64) - x["sed"]).max() <= 1 + 1e-4 * np.abs(x["sed"]).max()
     assert out[60][2].sum() > 0, "erosion never picked up sediment"
+
+
+def test_terrain_snapshot_follows_a_unit_change(oracle_lib):
+    """A parameter change that changes the height unit (the mass) has the
+    next step's snapshot at base + delta * new unit everywhere."""
+    prm, heights, pos, vel = _terrain_case(oracle_lib)
+    d, w = heights.shape
+    with S.System() as sysm:
+        sc = sysm.scene(S.default_params(**prm), capacity=len(pos), terrain=(w, d))
+        sc.set_terrain(heights)
+        sc.set_particles(pos, vel)
+        sysm.step(20)
+        p = sc.params()
+        p.mass = p.mass * 1.5
+        sc.set_params(p)
+        sysm.step(1)
+        hg, dl = sc.get_terrain()
+    hu = height_unit(dict(prm, mass=float(np.float32(prm["mass"]) * np.float32(1.5))), (w, d))
+    assert dl.any() and np.array_equal(hg, heights.astype(np.float32) + dl.astype(np.float32) * hu)
 
 
 def test_diag_fp64_sums(golden):
