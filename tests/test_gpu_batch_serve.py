@@ -57,6 +57,37 @@ def test_batched_equals_alone_bitwise():
         assert dg["total_units"] == 0 and rdg["total_units"] == 0
 
 
+def test_host_changes_between_steps_match_a_fresh_system(tmp_path):
+    """New particles and then a new grid between steps give what a fresh
+    system gives from the same state (its terrain from a checkpoint)."""
+    r = SMALL[1]
+    ck = str(tmp_path / "s.sphe")
+    with S.System(tile=128) as sysm:
+        sc = sysm.scene_from_request(W.base_params(), r)
+        sysm.step(9)
+        sc.save(ck)
+        st = sc.get_particles()
+        pos = st["pos"] + np.float32(0.001)
+        sc.set_particles(pos, st["vel"])
+        sysm.step(5)
+        p = sc.params()
+        p.cell_mult = 1.0
+        sc.set_params(p)
+        sysm.step(6)
+        got = _state(sc)
+    with S.System(tile=128) as ref:
+        sc = ref.scene_from_request(W.base_params(), r)
+        sc.load(ck)
+        sc.set_particles(pos, st["vel"])
+        ref.step(5)
+        p = sc.params()
+        p.cell_mult = 1.0
+        sc.set_params(p)
+        ref.step(6)
+        for a, b in zip(got, _state(sc)):
+            assert np.array_equal(a, b)
+
+
 def test_diag_many_and_state_fingerprint(tmp_path):
     """One diagnostic launch over several scenes gives each scene's own
     diagnostics; the state fingerprint does not depend on where the particles

@@ -177,6 +177,23 @@ def test_keys_and_sorted_order_bit_exact(golden, oracle_lib, cell_mult):
     assert np.array_equal(cnt, O.neighbour_counts(pos, 0.04))
 
 
+@pytest.mark.parametrize("variant", [None, 164088])
+def test_keys_after_steps_match_the_oracle(golden, oracle_lib, variant):
+    """After steps, the sort's cell keys equal the oracle's from the
+    current positions and its order ascends by key."""
+    O = oracle_lib
+    g = golden("ref_c1_16384.npz")
+    with S.System(particle_capacity=len(g["pos0"]), variant=variant) as sysm:
+        sc = sysm.scene(S.default_params(**C1, cell_mult=0.5))
+        sc.set_particles(g["pos0"])
+        sysm.step(23)
+        keys, order = sc.debug_sort()
+        pos = sc.get_particles()["pos"]
+    grd = O.grid(O.make_params(box_l=(0.5, 0.5, 0.5), h=0.04), 0.5)
+    assert np.array_equal(keys, O.cell_keys(grd, pos))
+    assert np.all(np.diff(keys[order].astype(np.int64)) >= 0)
+
+
 def test_edge_cases_match_reference(oracle_lib, golden):
     O = oracle_lib
     g = golden("ref_edge.npz")
