@@ -206,7 +206,7 @@ void oracle_neighbour_counts(int n, const float* pos, float h, int* counts, int 
     }
 }
 
-/* ---- uniform grid: row keys and stable counting sort ---------------------- */
+/* ---- uniform grid: Morton-row keys and stable counting sort --------------- */
 
 /* Cell edge = h * cell_mult * (1 + 2^-12): the small slack guarantees that two
  * particles within h never land more than ceil(1/cell_mult) cells apart after
@@ -236,19 +236,56 @@ static int cell_coord(float x, float lo, float inv, int n) {
     return (int)t;
 }
 
-/* row index of cell row (y, z), y fastest; the key is row * nx + x */
-static uint32_t yz_row(int cy, int cz, int ny) { return (uint32_t)cy + (uint32_t)cz * (uint32_t)ny; }
+static int bits_for(int n) {
+    int b = 0;
+    while ((1 << b) < n) b++;
+    return b;
+}
 
-uint32_t oracle_cell_key(const oracle_grid* g, float x, float y, float z) {
-    int cx = cell_coord(x, g->lo[0], g->inv_cell, g->nx);
-    int cy = cell_coord(y, g->lo[1], g->inv_cell, g->ny);
-    int cz = cell_coord(z, g->lo[2], g->inv_cell, g->nz);
-    return yz_row(cy, cz, g->ny) * (uint32_t)g->nx + (uint32_t)cx;
+/* (y, z) Morton code: bit b of y, then bit b of z, while each still has bits */
+static uint32_t yz_morton(int cy, int cz, int by, int bz) {
+    uint32_t m = 0;
+    int b, o = 0;
+    int top = by > bz ? by : bz;
+    for (b = 0; b < top; b++) {
+        if (b < by) m |= (uint32_t)((cy >> b) & 1) << o++;
+        if (b < bz) m |= (uint32_t)((cz >> b) & 1) << o++;
+    }
+    return m;
+}
+
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : x > y;
+}
+
+/* Row numbers: the ny * nz cell rows in (y, z) Morton order, numbered
+ * densely; rank[z * ny + y] = the number of row (y, z).  The key of a cell is
+ * rank * nx + x. */
+static uint32_t* row_ranks(const oracle_grid* g) {
+    size_t nr = (size_t)g->ny * g->nz, r;
+    int y, z, by = bits_for(g->ny), bz = bits_for(g->nz);
+    uint64_t* rows = (uint64_t*)malloc(nr * sizeof(uint64_t));
+    uint32_t* rank = (uint32_t*)malloc(nr * sizeof(uint32_t));
+    for (z = 0; z < g->nz; z++)
+        for (y = 0; y < g->ny; y++)
+            rows[(size_t)z * g->ny + y] = ((uint64_t)yz_morton(y, z, by, bz) << 32) | (uint64_t)((size_t)z * g->ny + y);
+    qsort(rows, nr, sizeof(uint64_t), cmp_u64);
+    for (r = 0; r < nr; r++) rank[rows[r] & 0xffffffffu] = (uint32_t)r;
+    free(rows);
+    return rank;
 }
 
 void oracle_cell_keys(const oracle_grid* g, int n, const float* pos, uint32_t* keys) {
+    uint32_t* rank = row_ranks(g);
     int i;
-    for (i = 0; i < n; i++) keys[i] = oracle_cell_key(g, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    for (i = 0; i < n; i++) {
+        int cx = cell_coord(pos[3 * i], g->lo[0], g->inv_cell, g->nx);
+        int cy = cell_coord(pos[3 * i + 1], g->lo[1], g->inv_cell, g->ny);
+        int cz = cell_coord(pos[3 * i + 2], g->lo[2], g->inv_cell, g->nz);
+        keys[i] = rank[(size_t)cz * g->ny + cy] * (uint32_t)g->nx + (uint32_t)cx;
+    }
+    free(rank);
 }
 
 void oracle_stable_sort(int n, const uint32_t* keys, int nkeys, int* perm) {

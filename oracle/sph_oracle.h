@@ -97,7 +97,7 @@ double oracle_time_sample(const oracle_params* p, int n, const float* pos, const
 /* Neighbour counts with the reference's test |x_i - x_j| <= h, j != i. */
 void oracle_neighbour_counts(int n, const float* pos, float h, int* counts, int nthreads);
 
-/* Uniform-grid restatement: cell dims, row keys and stable order. */
+/* Uniform-grid restatement: cell dims, Morton-row keys and stable order. */
 typedef struct oracle_grid {
     int nx, ny, nz;
     int nkeys;         /* nx * ny * nz, plus one sentinel key */
@@ -106,7 +106,6 @@ typedef struct oracle_grid {
     float lo[3];       /* grid origin (box minimum) */
 } oracle_grid;
 void oracle_grid_make(const oracle_params* p, float cell_mult, oracle_grid* g);
-uint32_t oracle_cell_key(const oracle_grid* g, float x, float y, float z);
 void oracle_cell_keys(const oracle_grid* g, int n, const float* pos, uint32_t* keys);
 /* perm[r] = index of the r-th particle in (key, index) order. */
 void oracle_stable_sort(int n, const uint32_t* keys, int nkeys, int* perm);

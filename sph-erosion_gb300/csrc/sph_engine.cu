@@ -36,9 +36,38 @@ inline int float_to_bits(float f) {
 
 }  // namespace
 
-// Row index of cell row (y, z): y + z * ny (rows of one z-slab adjacent,
-// no padding of the key space).
-uint32_t yz_row(int cy, int cz, int ny) { return (uint32_t)cy + (uint32_t)cz * (uint32_t)ny; }
+namespace {
+int bits_for(int n) {
+    int b = 0;
+    while ((1 << b) < n) ++b;
+    return b;
+}
+
+// (y, z) Morton code: bit b of y, then bit b of z, while each still has bits.
+uint32_t yz_morton(int cy, int cz, int by, int bz) {
+    uint32_t m = 0;
+    int o = 0;
+    for (int b = 0; b < std::max(by, bz); ++b) {
+        if (b < by) m |= (uint32_t)((cy >> b) & 1) << o++;
+        if (b < bz) m |= (uint32_t)((cz >> b) & 1) << o++;
+    }
+    return m;
+}
+}  // namespace
+
+// Row numbers of a grid's cell rows: the ny * nz rows (y, z) ordered along
+// the (y, z) Morton curve and numbered densely in that order, so that
+// neighbouring rows stay close in the sorted particle order while the key
+// space holds no codes outside the grid; tab[z * ny + y] = the row's number.
+void row_table(int ny, int nz, uint32_t* tab) {
+    const int by = bits_for(ny), bz = bits_for(nz);
+    std::vector<std::pair<uint32_t, uint32_t>> rows((size_t)ny * nz);
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            rows[(size_t)z * ny + y] = {yz_morton(y, z, by, bz), (uint32_t)((size_t)z * ny + y)};
+    std::sort(rows.begin(), rows.end());
+    for (size_t r = 0; r < rows.size(); ++r) tab[rows[r].second] = (uint32_t)r;
+}
 
 // Largest float s with sqrtf(s) <= h.  sqrtf is correctly rounded and
 // monotonic, so for every float s >= 0: sqrtf(s) <= h  <=>  s <= smax.  The
@@ -412,7 +441,7 @@ void System::geometry(Scene& sc) {
     sc.nkeys = (int)nk;
     sc.k_cap = (int)round_up(nk, kChunk);
     sc.nchunks = sc.k_cap / kChunk;
-    sc.tab_len = sc.ny + sc.nz;
+    sc.tab_len = sc.ny * sc.nz;
     sc.reach = (int)std::ceil(1.0 / (double)p.cell_mult - 1e-9);
 }
 
@@ -578,8 +607,7 @@ int System::create_scene(const sph_params& p, int capacity, int tw, int td) {
     }
     // row tables and clean key ranges
     std::vector<uint32_t> tab(sc.tab_len);
-    for (int y = 0; y < sc.ny; ++y) tab[y] = yz_row(y, 0, sc.ny);
-    for (int z = 0; z < sc.nz; ++z) tab[sc.ny + z] = yz_row(0, z, sc.ny);
+    row_table(sc.ny, sc.nz, tab.data());
     SPH_CK(cudaMemcpyAsync(tab_.p + sc.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
     SPH_CK(cudaMemsetAsync(counts_.p + sc.k_off, 0, (size_t)sc.k_cap * 4, st_));
     SPH_CK(cudaMemsetAsync(chunk_.p + sc.c_off, 0, (size_t)sc.nchunks * 4, st_));
@@ -645,8 +673,7 @@ void System::set_params(int id, const sph_params& p) {
             g.c_off = co;
             g.tab_off = to;
             std::vector<uint32_t> tab(g.tab_len);
-            for (int y = 0; y < g.ny; ++y) tab[y] = yz_row(y, 0, g.ny);
-            for (int z = 0; z < g.nz; ++z) tab[g.ny + z] = yz_row(0, z, g.ny);
+            row_table(g.ny, g.nz, tab.data());
             SPH_CK(cudaMemcpyAsync(tab_.p + g.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
             SPH_CK(cudaMemsetAsync(counts_.p + g.k_off, 0, (size_t)g.k_cap * 4, st_));
             SPH_CK(cudaMemsetAsync(chunk_.p + g.c_off, 0, (size_t)g.nchunks * 4, st_));
@@ -662,8 +689,7 @@ void System::set_params(int id, const sph_params& p) {
         }
     } else if (ng.nx != sc.nx || ng.ny != sc.ny || ng.nz != sc.nz) {
         std::vector<uint32_t> tab(ng.tab_len);
-        for (int y = 0; y < ng.ny; ++y) tab[y] = yz_row(y, 0, ng.ny);
-        for (int z = 0; z < ng.nz; ++z) tab[ng.ny + z] = yz_row(0, z, ng.ny);
+        row_table(ng.ny, ng.nz, tab.data());
         SPH_CK(cudaMemcpyAsync(tab_.p + ng.tab_off, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st_));
     }
     if ((p.flags & SPH_FLAG_RECORD) && rec_.n == 0) {

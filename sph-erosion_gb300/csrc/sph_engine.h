@@ -230,8 +230,9 @@ void fbm_heights(uint64_t seed, int w, int d, int octaves, float amplitude, floa
 
 // Sets the calling thread's sph_last_error() message (sph_capi.cu).
 void set_last_error(const std::string& msg);
-// Row-table entry of cell row (y, z): y + z * ny.
-uint32_t yz_row(int cy, int cz, int ny);
+// Morton-ordered dense row numbers of an ny x nz grid of cell rows:
+// tab[z * ny + y] for row (y, z).
+void row_table(int ny, int nz, uint32_t* tab);
 
 // Terrain meshes (sph_mesh.cu).
 void mesh_u8(const unsigned char* map_host, int dimx, int dimy, int dimz, float* verts, unsigned* idx,

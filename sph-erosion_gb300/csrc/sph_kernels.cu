@@ -6,7 +6,7 @@
 //
 // Stage order per step (the reference's Run, Erosion/fluid_system.h:104-183,
 // with its three O(N^2) passes replaced by a uniform grid):
-//   keys -> scan -> scatter -> reorder   counting sort into cell rows along x
+//   keys -> scan -> scatter -> reorder   counting sort into Morton-ordered cell rows along x
 //   density                               pass 1 (:107-124)
 //   force                                 passes 2 and 3 (:127-178), advance
 //                                         (:306-353), box (:355-407), terrain
@@ -76,7 +76,7 @@ __device__ __forceinline__ Cell cell_of(const SceneDev& S, float x, float y, flo
 }
 
 __device__ __forceinline__ uint32_t row_key(const uint32_t* tab, const SceneDev& S, int cy, int cz) {
-    return (__ldg(tab + S.tab_off + cy) + __ldg(tab + S.tab_off + S.ny + cz)) * (uint32_t)S.nx;
+    return __ldg(tab + S.tab_off + cz * S.ny + cy) * (uint32_t)S.nx;
 }
 
 // A particle's position in cell units before flooring and clamping, and its
@@ -162,11 +162,10 @@ __device__ __forceinline__ void for_rows_r(const DevArrays& a, const SceneDev& S
         const int z = q.c.cz + dz;
         const bool zin = live && z >= 0 && z < S.nz;
         float gz2 = INFINITY;
-        uint32_t kz = 0;
+        const uint32_t* tz = tab + (zin ? z : 0) * S.ny;  // row numbers of slab z
         if (zin) {
             const float g = cell_gap(q.tz, z, S.nz);
             gz2 = g * g;
-            kz = __ldg(tab + S.ny + z);
         }
 #pragma unroll 1
         for (int dy = -R; dy <= R; ++dy) {
@@ -182,7 +181,7 @@ __device__ __forceinline__ void for_rows_r(const DevArrays& a, const SceneDev& S
                         if (gx2[R - d] <= r2) lo = -d;
                         if (gx2[R + d] <= r2) hi = d;
                     }
-                    const uint32_t row = (__ldg(tab + y) + kz) * (uint32_t)S.nx;
+                    const uint32_t row = __ldg(tz + y) * (uint32_t)S.nx;
                     st = __ldg(off + row + q.c.cx + lo);
                     en = __ldg(off + row + q.c.cx + hi + 1);
                 }

@@ -144,8 +144,7 @@ extern "C" SPH_API int sph_density_static(const sph_params* p, int n, const floa
         for (int t = 0; t * kStaticTile < n; ++t) pt.push_back({0, t * kStaticTile});
         for (int c = 0; c < sc.nchunks; ++c) ct.push_back({0, c});
         std::vector<uint32_t> tab(sc.tab_len);
-        for (int y = 0; y < sc.ny; ++y) tab[y] = yz_row(y, 0, sc.ny);
-        for (int z = 0; z < sc.nz; ++z) tab[sc.ny + z] = yz_row(0, z, sc.ny);
+        row_table(sc.ny, sc.nz, tab.data());
         const int steps = -1;
         const int nwork[4] = {(int)pt.size(), (int)ct.size(), 0, 0};
         check_cuda(cudaMemcpyAsync(base + kOffScene, &sc.dev, sizeof(SceneDev), cudaMemcpyHostToDevice, st), "copy");

@@ -33,7 +33,7 @@ struct SceneDev {
     int k_off, nkeys, k_cap; // keys [k_off, k_off + nkeys), nkeys includes the end sentinel
     int c_off, nchunks;      // scan chunk sums
     int t_off, tw, td;       // terrain vertices (tw along x, td along z)
-    int tab_off;             // row tables: y at tab_off, z * ny at tab_off + ny (row = sum)
+    int tab_off;             // row numbers (Morton order): row (y, z) at tab_off + z * ny + y
     int nx, ny, nz, reach;   // cell grid and stencil reach in cells
     int flags;
     int pad0;
