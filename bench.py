@@ -364,6 +364,41 @@ def init_dist(ws):
             dist.init_process_group("gloo")
 
 
+def run_long(args, spec, config):
+    """The configured run of a plain workload from its first step: --steps
+    steps in chunks of --mass-every (16-step graphs, no flush: the rainfall
+    state is far larger than L2), each chunk timed with CUDA events and
+    followed (untimed) by the exact-mass check of the diagnostics.  One
+    line: steps over the summed chunk times, and every check's units."""
+    import torch
+
+    import sph_gb300 as S
+    import workloads as W
+
+    torch.cuda.set_device(0)
+    n = spec["n"]
+    with S.System(particle_capacity=n, key_capacity=1 << 20, terrain_capacity=1 << 21, tile=args.tile,
+                  graph_steps=16, variant=args.variant) as sysm:
+        sc = W.build_scene(sysm, dict(spec, params=dict(spec["params"], cell_mult=args.cell_mult)))
+        d0 = sc.diag()
+        ms, checks, done = 0.0, [], 0
+        with Clocks() as clk:
+            while done < args.steps:
+                k = min(args.mass_every, args.steps - done)
+                ms += sysm.time_steps(k)
+                done += k
+                d = sc.diag()
+                checks.append(int(d["total_units"]))
+        line = {"metric": "particle-steps/s of the configured run", "value": n * done / (ms * 1e-3),
+                "unit": "particle-steps/s", "n_gpus": 1, "steps": done, "ms_per_step": ms / done,
+                "wall_gpu_s": ms / 1e3, "config": dict(config, window=f"steps 1..{done}", l2="state larger than L2",
+                                                       variant=args.variant, tile=args.tile, cell_mult=args.cell_mult),
+                "mass_checks": {"every": args.mass_every, "total_units": checks,
+                                "exact": all(c == 0 for c in checks) and d0["total_units"] == 0},
+                "nan_particles": int(d["nan_particles"]), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, spec, config):
     import torch
 
@@ -763,6 +798,10 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="serving: requests in the trace")
+    ap.add_argument("--long", action="store_true",
+                    help="plain workloads: the configured run from step 1 (--steps steps, no spin-up), in timed "
+                         "chunks with an exact-mass check after each (e.g. --workload skew --steps 10000)")
+    ap.add_argument("--mass-every", type=int, default=500, help="with --long: steps between mass checks")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per second")
     ap.add_argument("--policy", default="work", choices=["arrival", "work"],
                     help="serving: admission order among arrived requests (least work first by default)")
@@ -817,6 +856,8 @@ def main():
                         f"after {spinup_steps(args)} untimed spin-up steps"}
     if args.impl == "reference":
         run_reference(args, spec, config)
+    elif args.long:
+        run_long(args, spec, config)
     else:
         run_ours(args, spec, config)
 
