@@ -390,6 +390,14 @@ __device__ __forceinline__ void force_pair(const SceneDev& S, ForceAcc& acc, flo
 // for 1/|r|.  The in-range test stays exact (s <= smax), so the neighbour sets
 // and NeighbId are the reference's; the rounding is not, and the results are
 // held to the parity tolerance instead of to bits.
+//
+// r^2 with two fused multiply-adds, the force pass's fast form (its pairs
+// are in range already): like dist2, within 3 units of rounding of the true
+// sum of squares.
+__device__ __forceinline__ float dist2_fma(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
 __device__ __forceinline__ float density_term_fast(const SceneDev& S, float s) {
     const float hs = S.hh - s;
     return (S.mass * S.c_poly6) * (hs * hs * hs);
@@ -949,7 +957,7 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
         const float4* sd = a.dyn + S.p_off;
         auto pair_with = [&](uint32_t j, float4 xj, float4 vj, float4 dj) {
             const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
-            const float s = dist2(rx, ry, rz);
+            const float s = FM ? dist2_fma(rx, ry, rz) : dist2(rx, ry, rz);
             if (FM)
                 force_pair_fast(S, acc, rx, ry, rz, s, vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z, __float_as_int(xj.w),
                                 (int)j == pl);
@@ -1028,7 +1036,7 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
                     const int idj = rec ? __float_as_int(__ldg(&sp[j0].w)) : 0;
                     const float rx = fs(xi.x, a0.x), ry = fs(xi.y, a0.y), rz = fs(xi.z, a0.z);
                     if (FM)
-                        force_pair_fast(S, acc, rx, ry, rz, dist2(rx, ry, rz), vi.x, vi.y, vi.z, Ai, b0, a0.w, b0.w,
+                        force_pair_fast(S, acc, rx, ry, rz, dist2_fma(rx, ry, rz), vi.x, vi.y, vi.z, Ai, b0, a0.w, b0.w,
                                         idj, (int)j0 == pl);
                     else
                         force_pair(S, acc, rx, ry, rz, fsq(dist2(rx, ry, rz)), vi.x, vi.y, vi.z, Ai, b0, a0.w, b0.w,
@@ -1450,7 +1458,7 @@ __global__ void __launch_bounds__(kMaxTile + 32, MINB) k_force_tma(DevArrays a, 
                     const uint32_t j = jring[(size_t)st * T + tid];
                     const int idj = rec ? __float_as_int(__ldg(&sp[j].w)) : 0;
                     const float rx = fs(xi.x, r0.x), ry = fs(xi.y, r0.y), rz = fs(xi.z, r0.z);
-                    force_pair_fast(S, acc, rx, ry, rz, dist2(rx, ry, rz), vi.x, vi.y, vi.z, Ai, r1, r0.w, r1.w, idj,
+                    force_pair_fast(S, acc, rx, ry, rz, dist2_fma(rx, ry, rz), vi.x, vi.y, vi.z, Ai, r1, r0.w, r1.w, idj,
                                     (int)j == pl);
                 }
                 __syncwarp();
@@ -1462,10 +1470,9 @@ __global__ void __launch_bounds__(kMaxTile + 32, MINB) k_force_tma(DevArrays a, 
                 const float4* sd = a.dyn + S.p_off;
                 for_each_candidate(a, S, xi, [&](uint32_t j, float4 xj) {
                     const float rx = fs(xi.x, xj.x), ry = fs(xi.y, xj.y), rz = fs(xi.z, xj.z);
-                    const float s2 = dist2(rx, ry, rz);
-                    if (s2 <= S.smax) {
+                    if (dist2(rx, ry, rz) <= S.smax) {
                         const float4 vj = __ldg(sv + j), dj = __ldg(sd + j);
-                        force_pair_fast(S, acc, rx, ry, rz, s2, vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z,
+                        force_pair_fast(S, acc, rx, ry, rz, dist2_fma(rx, ry, rz), vi.x, vi.y, vi.z, Ai, vj, dj.y, dj.z,
                                         __float_as_int(xj.w), (int)j == pl);
                     }
                 });

@@ -309,6 +309,31 @@ def test_fast_arithmetic_forms_identical(golden):
             assert np.array_equal(got[s][1], base[s][1]), (v, s)
 
 
+def test_fast_in_range_test_is_exact_at_the_boundary():
+    """Fast arithmetic keeps the reference's in-range test: isolated pairs
+    at distances within 20 units of rounding of h, in random 3-D
+    directions, are in range for the fast passes exactly when they are for
+    the reference-order passes (NeighbId of each pair's first particle)."""
+    rng = np.random.default_rng(17)
+    h = np.float32(C1["smoothing_radius"])
+    m = 1500
+    side = int(np.ceil(m ** (1 / 3)))
+    g = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:m]
+    a = ((g - side / 2) * 0.15).astype(np.float32)
+    d = rng.normal(size=(m, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    t = rng.integers(-20, 21, m)
+    r = (float(h) * (1.0 + t * 2.0 ** -24))[:, None] * d
+    b = (a + r).astype(np.float32)
+    pos = np.concatenate([a, b])  # pair k: ids k and m + k
+    prm = dict(C1, box_half=(1.0, 1.0, 1.0))
+    exact = run(prm, pos, 1, variant=216)[1][1]
+    fast = run(prm, pos, 1, variant=164088)[1][1]
+    assert np.array_equal(fast, exact)
+    linked = exact[:m] == np.arange(m) + m
+    assert 0 < linked.sum() < m  # both sides of the boundary are present
+
+
 def test_cooperative_overflow_path():
     """Particles with more in-range neighbours than a list holds: the
     cooperative force pass splits their cell rows over the group instead;
