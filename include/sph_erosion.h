@@ -437,8 +437,8 @@ SPH_API int sph_server_run_trace(sph_server* s, const sph_request* reqs, int n, 
  * streams or host threads) race and must be serialised by the caller. */
 #define SPH_STATIC_MAX_PARTICLES 32768
 #define SPH_STATIC_MAX_KEYS 262144
-#define SPH_STATIC_MAX_TABLE 4096
-#define SPH_STATIC_SCRATCH_BYTES 5131008
+#define SPH_STATIC_MAX_TABLE 262144 /* row numbers: ny * nz <= SPH_STATIC_MAX_KEYS */
+#define SPH_STATIC_SCRATCH_BYTES 6163200
 SPH_API int sph_density_static(const sph_params* p, int n, const float* pos3_dev, float* density_dev,
                                float* pressure_dev, void* stream);
 
