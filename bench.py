@@ -72,7 +72,7 @@ KERNEL_SOURCES = ("sph_kernels.cu", "sph_kernels.h", "sph_types.h")
 
 def source_digest() -> str:
     """Digest of the kernels' source files: counters captured from another
-    build of the kernels are not reported as this build's."""
+    build of the kernels are not reported as the current kernels'."""
     h = hashlib.sha256()
     for f in KERNEL_SOURCES:
         with open(os.path.join(ROOT, "sph-erosion_gb300", "csrc", f), "rb") as fh:

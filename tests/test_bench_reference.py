@@ -79,7 +79,7 @@ def test_ncu_counters_ingest_and_match(tmp_path, monkeypatch):
     assert bench.ncu_counters("plain_1m", v & ~64, 0.5, "k_force")[0] is not None
     assert bench.ncu_counters("plain_1m", v & ~64, 0.5, "k_density")[0] is None
     assert bench.ncu_counters("plain_1m", v, 1.0, "k_force")[0] is None
-    # counters of other kernel sources are not reported as this build's
+    # counters of other kernel sources are not reported as the current kernels'
     monkeypatch.setattr(bench, "source_digest", lambda: "0" * 16)
     e, why = bench.ncu_counters("plain_1m", v, 0.5, "k_force")
     assert e is None and "other kernel sources" in why
