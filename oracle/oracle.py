@@ -40,6 +40,7 @@ class OracleGrid(C.Structure):
     _fields_ = [
         ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
         ("nkeys", C.c_int), ("cell", C.c_float), ("inv_cell", C.c_float), ("lo", C.c_float * 3),
+        ("inv_cell_x", C.c_float),
     ]
 
 

@@ -208,17 +208,23 @@ void oracle_neighbour_counts(int n, const float* pos, float h, int* counts, int 
 
 /* ---- uniform grid: Morton-row keys and stable counting sort --------------- */
 
-/* Cell edge = h * cell_mult * (1 + 2^-12): the small slack guarantees that two
- * particles within h never land more than ceil(1/cell_mult) cells apart after
- * FP32 rounding of the key arithmetic. */
+/* Cell edge along y and z = h * cell_mult * (1 + 2^-12); along x the same
+ * over xsub = 2 when the reach ceil(1/cell_mult) is 1, else over 1.  The
+ * small slack guarantees that two particles within h never land more than
+ * the reach apart along y and z (reach * xsub along x) after FP32 rounding
+ * of the key arithmetic. */
 void oracle_grid_make(const oracle_params* p, float cell_mult, oracle_grid* g) {
     int a;
     int dims[3];
+    int reach = (int)ceil(1.0 / (double)cell_mult - 1e-9);
+    int xsub = reach == 1 ? 2 : 1;
     g->cell = (p->h * cell_mult) * 1.000244140625f;
     g->inv_cell = 1.0f / g->cell;
+    g->inv_cell_x = g->inv_cell * (float)xsub;
     for (a = 0; a < 3; a++) {
         float ext = p->box_l[a] + p->box_l[a];
-        int nd = (int)ceil((double)ext / (double)g->cell);
+        float edge = a == 0 ? g->cell / (float)xsub : g->cell;
+        int nd = (int)ceil((double)ext / (double)edge);
         if (nd < 1) nd = 1;
         dims[a] = nd;
         g->lo[a] = p->box_c[a] - p->box_l[a];
@@ -280,7 +286,7 @@ void oracle_cell_keys(const oracle_grid* g, int n, const float* pos, uint32_t* k
     uint32_t* rank = row_ranks(g);
     int i;
     for (i = 0; i < n; i++) {
-        int cx = cell_coord(pos[3 * i], g->lo[0], g->inv_cell, g->nx);
+        int cx = cell_coord(pos[3 * i], g->lo[0], g->inv_cell_x, g->nx);
         int cy = cell_coord(pos[3 * i + 1], g->lo[1], g->inv_cell, g->ny);
         int cz = cell_coord(pos[3 * i + 2], g->lo[2], g->inv_cell, g->nz);
         keys[i] = rank[(size_t)cz * g->ny + cy] * (uint32_t)g->nx + (uint32_t)cx;

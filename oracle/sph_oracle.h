@@ -101,9 +101,10 @@ void oracle_neighbour_counts(int n, const float* pos, float h, int* counts, int 
 typedef struct oracle_grid {
     int nx, ny, nz;
     int nkeys;         /* nx * ny * nz, plus one sentinel key */
-    float cell;        /* cell edge */
+    float cell;        /* cell edge along y and z; along x cell / xsub (2 at reach 1, else 1) */
     float inv_cell;
     float lo[3];       /* grid origin (box minimum) */
+    float inv_cell_x;  /* xsub * inv_cell */
 } oracle_grid;
 void oracle_grid_make(const oracle_params* p, float cell_mult, oracle_grid* g);
 void oracle_cell_keys(const oracle_grid* g, int n, const float* pos, uint32_t* keys);

@@ -418,18 +418,24 @@ void System::ensure_arena(RangeAlloc& ra, int64_t need, int which) {
     }
 }
 
-// Uniform grid of a scene.  Cell edge = h * cell_mult * (1 + 2^-12); the
-// slack keeps any two particles within h at most `reach` cells apart after
-// the FP32 rounding of the key arithmetic, so the traversal never misses a
-// neighbour.
+// Uniform grid of a scene.  Cell edge along y and z = h * cell_mult *
+// (1 + 2^-12); along x the same over xsub, 2 when one cell is h or more
+// (reach 1: rows are then trimmed to the sphere in half cells), else 1
+// (exact either way: a power of two).  The slack keeps any two particles
+// within h at most `reach` cells apart along y and z, and reach * xsub along
+// x, after the FP32 rounding of the key arithmetic, so the traversal never
+// misses a neighbour.
 void System::geometry(Scene& sc) {
     const sph_params& p = sc.prm;
     sc.cell = (p.smoothing_radius * p.cell_mult) * 1.000244140625f;
     sc.inv_cell = 1.0f / sc.cell;
+    sc.reach = (int)std::ceil(1.0 / (double)p.cell_mult - 1e-9);
+    sc.xsub = sc.reach == 1 ? 2 : 1;
     int d[3];
     for (int a = 0; a < 3; ++a) {
         const float ext = p.box_half[a] + p.box_half[a];
-        int nd = (int)std::ceil((double)ext / (double)sc.cell);
+        const float edge = a == 0 ? sc.cell / (float)sc.xsub : sc.cell;
+        int nd = (int)std::ceil((double)ext / (double)edge);
         d[a] = std::max(nd, 1);
         sc.lo[a] = p.box_center[a] - p.box_half[a];
     }
@@ -442,7 +448,6 @@ void System::geometry(Scene& sc) {
     sc.k_cap = (int)round_up(nk, kChunk);
     sc.nchunks = sc.k_cap / kChunk;
     sc.tab_len = sc.ny * sc.nz;
-    sc.reach = (int)std::ceil(1.0 / (double)p.cell_mult - 1e-9);
 }
 
 void System::fill_dev(Scene& sc) {
@@ -472,6 +477,8 @@ void System::fill_dev(Scene& sc) {
     if (p.flags & SPH_FLAG_ORDERED) d.flags |= kFlagOrdered;
     for (int a = 0; a < 3; ++a) d.lo[a] = sc.lo[a];
     d.inv_cell = sc.inv_cell;
+    d.inv_cell_x = sc.inv_cell * (float)sc.xsub;  // exact: 1 / (cell / xsub)
+    d.xsub = sc.xsub;
     // h in cell units for the row trimming, enlarged by 1e-5 relative plus four
     // ulps of the largest in-grid cell coordinate, so that the FP32 rounding of
     // the two particles' cell coordinates can never drop a neighbour

@@ -68,7 +68,7 @@ struct Scene {
     int n = 0;
     int p_cap = 0;
     int64_t p_off = 0;
-    int nx = 1, ny = 1, nz = 1, reach = 1;
+    int nx = 1, ny = 1, nz = 1, reach = 1, xsub = 1;
     int nkeys = 0, k_cap = 0, nchunks = 0;
     int64_t k_off = 0, c_off = 0, tab_off = 0;
     int tab_len = 0;

@@ -78,7 +78,7 @@ struct Cell {
 
 __device__ __forceinline__ Cell cell_of(const SceneDev& S, float x, float y, float z) {
     Cell c;
-    c.cx = cell_coord(x, S.lo[0], S.inv_cell, S.nx);
+    c.cx = cell_coord(x, S.lo[0], S.inv_cell_x, S.nx);
     c.cy = cell_coord(y, S.lo[1], S.inv_cell, S.ny);
     c.cz = cell_coord(z, S.lo[2], S.inv_cell, S.nz);
     return c;
@@ -98,7 +98,7 @@ struct Probe {
 
 __device__ __forceinline__ Probe probe_of(const SceneDev& S, float4 x) {
     Probe q;
-    q.tx = fm(fs(x.x, S.lo[0]), S.inv_cell);
+    q.tx = fm(fs(x.x, S.lo[0]), S.inv_cell_x);
     q.ty = fm(fs(x.y, S.lo[1]), S.inv_cell);
     q.tz = fm(fs(x.z, S.lo[2]), S.inv_cell);
     q.finite = (q.tx == q.tx) && (q.ty == q.ty) && (q.tz == q.tz);
@@ -125,7 +125,7 @@ __device__ __forceinline__ bool row_span(const SceneDev& S, const Probe& q, int 
     const float gy = cell_gap(q.ty, y, S.ny), gz = cell_gap(q.tz, z, S.nz);
     const float r2 = S.hcell * S.hcell - gy * gy - gz * gz;
     if (!(r2 >= 0.0f)) return false;
-    const float r = sqrtf(r2);
+    const float r = sqrtf(r2) * (float)S.xsub;  // in x cells
     const float top = (float)(S.nx - 1);
     const float lo = fminf(fmaxf(floorf(q.tx - r), 0.0f), top);
     const float hi = fminf(fmaxf(floorf(q.tx + r), 0.0f), top);
@@ -143,9 +143,11 @@ __device__ __forceinline__ bool row_span(const SceneDev& S, const Probe& q, int 
 // out-of-range candidates are ever dropped and the in-range visiting order is
 // that of the full (2R+1)^3 block.
 //
-// For R = 1 and 2 (cells of h and h/2) the squared gaps of the 2R+1 cells
-// along x are computed once per particle (registers), so a row costs a few
-// adds and compares; the row loops stay rolled to keep register pressure (and
+// At reach 1 (cells of h or more) cells along x are half as long as along y
+// and z (xsub 2): a row's range is trimmed to the sphere in finer steps at
+// no extra row.  For R = 1 and 2 (y/z cells of h and h/2, x reach 2 cells
+// either way) the squared gaps of the 5 x cells are computed once per
+// particle (registers), so a row costs a few adds and compares; the row loops stay rolled to keep register pressure (and
 // so occupancy) where these latency-bound kernels need it.  Other reaches
 // take the general path.
 template <int R, class Fn>
@@ -154,16 +156,18 @@ __device__ __forceinline__ void for_rows_r(const DevArrays& a, const SceneDev& S
     const uint32_t* off = a.offsets + S.k_off;
     const uint32_t* tab = a.tab + S.tab_off;
     const float H2 = S.hcell * S.hcell;
-    float gx2[2 * R + 1];
+    constexpr int XS = R == 1 ? 2 : 1;  // the scene's xsub at this reach
+    constexpr int RX = R * XS;          // reach along x, in x cells
+    float gx2[2 * RX + 1];              // squared x-gaps in y/z cell units
 #pragma unroll
-    for (int d = -R; d <= R; ++d) {
+    for (int d = -RX; d <= RX; ++d) {
         const int k = q.c.cx + d;
         float g2 = INFINITY;
         if (k >= 0 && k < S.nx) {
-            const float g = cell_gap(q.tx, k, S.nx);
+            const float g = cell_gap(q.tx, k, S.nx) * (1.0f / XS);
             g2 = g * g;
         }
-        gx2[d + R] = g2;
+        gx2[d + RX] = g2;
     }
     const bool live = valid && q.finite;
 #pragma unroll 1
@@ -186,9 +190,9 @@ __device__ __forceinline__ void for_rows_r(const DevArrays& a, const SceneDev& S
                 if (r2 >= 0.0f) {
                     int lo = 0, hi = 0;  // farthest reachable cell on each side
 #pragma unroll
-                    for (int d = 1; d <= R; ++d) {
-                        if (gx2[R - d] <= r2) lo = -d;
-                        if (gx2[R + d] <= r2) hi = d;
+                    for (int d = 1; d <= RX; ++d) {
+                        if (gx2[RX - d] <= r2) lo = -d;
+                        if (gx2[RX + d] <= r2) hi = d;
                     }
                     const uint32_t row = __ldg(tz + y) * (uint32_t)S.nx;
                     st = __ldg(off + row + q.c.cx + lo);
@@ -1065,8 +1069,8 @@ __global__ void __launch_bounds__(kMaxTile, MINB) k_force(DevArrays a) {
 // Range [st, en) of stencil row r of the particle at probe q: rows in the
 // order of for_rows (dz outer, dy inner, both ascending), trimmed the same
 // way, so a particle's candidates come in the same order.  gx2 holds the
-// squared x-gaps of cells cx - R .. cx + R (R = 1, 2; unused for R = 0, the
-// general reach).
+// squared x-gaps, in y/z cell units, of the x cells cx - 2 .. cx + 2 (R = 1
+// with xsub 2, R = 2 with xsub 1; unused for R = 0, the general reach).
 template <int R>
 __device__ __forceinline__ void stencil_row(const DevArrays& a, const SceneDev& S, const Probe& q, const float* gx2,
                                             int r, uint32_t& st, uint32_t& en) {
@@ -1082,10 +1086,11 @@ __device__ __forceinline__ void stencil_row(const DevArrays& a, const SceneDev& 
         const float r2 = S.hcell * S.hcell - gy * gy - gz * gz;
         if (!(r2 >= 0.0f)) return;
         int lo = 0, hi = 0;
+        constexpr int RX = (R > 0 ? R : 1) * (R == 1 ? 2 : 1);
 #pragma unroll
-        for (int d = 1; d <= (R > 0 ? R : 1); ++d) {
-            if (gx2[R - d] <= r2) lo = -d;
-            if (gx2[R + d] <= r2) hi = d;
+        for (int d = 1; d <= RX; ++d) {
+            if (gx2[RX - d] <= r2) lo = -d;
+            if (gx2[RX + d] <= r2) hi = d;
         }
         const uint32_t row = row_key(a.tab, S, y, z);
         st = __ldg(off + row + q.c.cx + lo);
@@ -1133,17 +1138,19 @@ __device__ __forceinline__ void density_coop_particle(const DevArrays& a, const 
                                                       const Group<G>& g) {
     const float4 xi = a.spos[p];
     const Probe q = probe_of(S, xi);
-    float gx2[2 * (R > 0 ? R : 1) + 1];
+    constexpr int XS = R == 1 ? 2 : 1;  // the scene's xsub at this reach
+    constexpr int RX = (R > 0 ? R : 1) * XS;
+    float gx2[2 * RX + 1];  // squared x-gaps in y/z cell units
     if (R > 0) {
 #pragma unroll
-        for (int d = -R; d <= R; ++d) {
+        for (int d = -RX; d <= RX; ++d) {
             const int k = q.c.cx + d;
             float g2 = INFINITY;
             if (k >= 0 && k < S.nx) {
-                const float gg = cell_gap(q.tx, k, S.nx);
+                const float gg = cell_gap(q.tx, k, S.nx) * (1.0f / XS);
                 g2 = gg * gg;
             }
-            gx2[d + R] = g2;
+            gx2[d + RX] = g2;
         }
     }
     const float4* sp = a.spos + S.p_off;

@@ -36,10 +36,11 @@ struct SceneDev {
     int tab_off;             // row numbers (Morton order): row (y, z) at tab_off + z * ny + y
     int nx, ny, nz, reach;   // cell grid and stencil reach in cells
     int flags;
-    int pad0;
+    int xsub;                // x cells per y/z cell: 2 at reach 1 (cells of h or more), else 1
     // grid
     float lo[3];
-    float inv_cell;
+    float inv_cell;          // per metre, along y and z
+    float inv_cell_x;        // per metre, along x: xsub * inv_cell
     float hcell;             // h in cell units, enlarged to cover FP32 rounding (row trimming)
     // physics (Erosion/fluid_system.h:460-479)
     float h, hh;             // h and h*h
