@@ -1501,15 +1501,28 @@ size_t force_tma_smem(int tile) {
 }
 
 // terrain: height snapshot = base + delta * unit, read by the next step.
-__global__ void __launch_bounds__(kMaxTile) k_terrain(DevArrays a) {
+// Four vertices per thread: a tile of T vertices takes T / 4 threads, each
+// with 16-byte loads and stores (a scene's vertices start on a 512-vertex
+// boundary, so every thread's first vertex is 4-aligned).
+__global__ void __launch_bounds__(kMaxTile / 4) k_terrain(DevArrays a) {
     const int nwork = *a.n_ttiles;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = a.ttiles[w];
         if (a.steps_left[wk.scene] == 0) continue;
         const SceneDev& S = a.scenes[wk.scene];
-        const int t = wk.start + threadIdx.x;
-        if (t >= S.t_off + S.tw * S.td) continue;
-        a.theight[t] = fa(a.tbase[t], fm(__ll2float_rn(a.tdelta[t]), S.height_unit));
+        const int t = wk.start + 4 * (int)threadIdx.x;
+        const int end = S.t_off + S.tw * S.td;
+        const float u = S.height_unit;
+        if (t + 3 < end) {
+            const float4 b = *reinterpret_cast<const float4*>(a.tbase + t);
+            const longlong2 d0 = *reinterpret_cast<const longlong2*>(a.tdelta + t);
+            const longlong2 d1 = *reinterpret_cast<const longlong2*>(a.tdelta + t + 2);
+            *reinterpret_cast<float4*>(a.theight + t) =
+                make_float4(fa(b.x, fm(__ll2float_rn(d0.x), u)), fa(b.y, fm(__ll2float_rn(d0.y), u)),
+                            fa(b.z, fm(__ll2float_rn(d1.x), u)), fa(b.w, fm(__ll2float_rn(d1.y), u)));
+        } else {
+            for (int k = t; k < end && k < t + 4; ++k) a.theight[k] = fa(a.tbase[k], fm(__ll2float_rn(a.tdelta[k]), u));
+        }
     }
 }
 
@@ -1890,7 +1903,7 @@ void launch_force_ordered(const DevArrays& a, const LaunchShape& s, cudaStream_t
     k_force<true, 1><<<s.grid_p, s.tile, 0, st>>>(a);
 }
 void launch_terrain(const DevArrays& a, const LaunchShape& s, cudaStream_t st) {
-    k_terrain<<<s.grid_t, s.tile, 0, st>>>(a);
+    k_terrain<<<s.grid_t, s.tile / 4, 0, st>>>(a);
 }
 void launch_tick(const DevArrays& a, int nscenes, cudaStream_t st) {
     k_tick<<<(nscenes + 127) / 128, 128, 0, st>>>(a.steps_left, nscenes);
