@@ -430,6 +430,21 @@ def test_terrain_erosion_parity_and_exact_mass(oracle_lib, ordered):
     assert out[60][2].sum() > 0, "erosion never picked up sediment"
 
 
+def test_terrain_snapshot_with_a_ragged_vertex_count(oracle_lib):
+    """A 35 x 33 terrain (1,155 vertices: the last tile ends three past a
+    multiple of four) eroded for 60 steps: every height of the snapshot is
+    base + delta * unit, the tail included."""
+    O = oracle_lib
+    prm, _, pos, vel = _terrain_case(O)
+    heights = O.fbm(11, 35, 33, 4, 0.08)
+    d, w = heights.shape
+    out = run_terrain(prm, pos, heights, 60, vel=vel)
+    _, _, sed, hg, dl, dg = out[60]
+    assert dl.any() and dg["total_units"] == 0
+    hu = height_unit(prm, (w, d))
+    assert np.array_equal(hg, heights.astype(np.float32) + dl.astype(np.float32) * hu)
+
+
 def test_terrain_snapshot_follows_a_unit_change(oracle_lib):
     """A parameter change that changes the height unit (the mass) has the
     next step's snapshot at base + delta * new unit everywhere."""
